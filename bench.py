@@ -1,0 +1,460 @@
+"""Benchmark: w-projection gridding + degridding throughput (Mvis/s) on one GB300.
+
+Workload (default): the 4,177,920-visibility w-projection observation
+(256 log-radial antennas, 32,640 baselines x 128 time samples, 4096^2
+complex64 grid, 32 w-planes with supports 8..64, oversample 8, w-kernels
+generated on the GPU in FP64 and cast to complex64), seeded synthetic data.
+
+One step = one gridding pass (zero the grid, grid every visibility) plus one
+degridding pass (predict every visibility from a model grid) through the
+FP32 tiled adjoint pair, replayed from a CUDA graph, inputs resident in HBM,
+L2 flushed (a 256 MiB write) before every step.  Reported next to it: the
+plain FP64 GPU path, the FP32 error against it, the HBM roofline of the
+dominant kernel, an end-to-end figure with host buffers, and the CPU
+restatement of the reference's gridder timed on the host cores.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Mvis/s grid+degrid, FP32 batched vs FP64 plain at stated err; % HBM roofline"
+L2_BYTES = 129 * 1024 * 1024
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 6:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx.append(float(f[1]))
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if f[2 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------- workload
+def load_workload(name):
+    from rc_gb300 import synth
+
+    return synth.config(name)
+
+
+def cpu_leg(ob, supports, gcf128_np, offs, sample_n, nthreads):
+    """The reference's CPU gridder semantics (the oracle's FP64 restatement,
+    multi-plane, per-thread grids as MS4's OpenMP gridder does) on the first
+    sample_n visibilities: grid, then degrid from the gridded result."""
+    from oracle import oracle as O
+
+    n = min(sample_n, ob.n)
+    uvw = np.ascontiguousarray(ob.uvw[:n])
+    vis = np.ascontiguousarray(ob.vis[:n])
+    plane = O.wbin(uvw, ob.w_low, ob.w_high, ob.n_planes)
+    G = ob.grid_size
+    grid = np.zeros((G, G), np.complex128)
+    t0 = time.perf_counter()
+    used = O.scatter_planes(ob.scale, G, int(supports.max()), uvw, vis, plane, supports,
+                            gcf128_np, offs, grid, nthreads=nthreads)
+    t1 = time.perf_counter()
+    O.degrid_planes(ob.scale, G, int(supports.max()), uvw, plane, supports, gcf128_np, offs, grid,
+                    mode=0, nthreads=nthreads)
+    t2 = time.perf_counter()
+    return n, (t2 - t0), used, (t1 - t0), (t2 - t1)
+
+
+def reference_arm(args):
+    """--impl reference: the reference's CPU gridding path (its semantics
+    restated in C, FP64, all host threads) on this workload; the reference's
+    own kernels are Halide generators that cannot be built here."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    from rc_gb300 import gcf as Gm
+
+    ob = load_workload(args.config)
+    offs, total = Gm.layout(ob.supports)
+    gcf = _gcf_host(ob)
+    nthreads = os.cpu_count() or 1
+    sample_n = args.cpu_sample
+    if args.warmup > 0:
+        cpu_leg(ob, ob.supports, gcf, offs, min(sample_n, 50000), nthreads)
+    times = []
+    for _ in range(args.steps):
+        n, dt, used, _, _ = cpu_leg(ob, ob.supports, gcf, offs, sample_n, nthreads)
+        times.append(dt)
+    t = float(np.mean(times))
+    val = n / t / 1e6
+    line = {
+        "metric": METRIC, "impl": "reference", "value": round(val, 3), "unit": "Mvis/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(1e3 * t, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+        "config": {"workload": _workload_desc(ob), "sample_visibilities": n},
+        "cpu_baseline": {"value": round(val, 3), "unit": "Mvis/s", "cores": used, "kind": "port",
+                         "sample": f"first {n} of {ob.n} visibilities, grid + degrid, FP64"},
+        "e2e": {"value": round(val, 3), "unit": "Mvis/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def _workload_desc(ob):
+    return (f"{ob.name}: {ob.n} vis, {ob.grid_size}^2 grid, {ob.n_planes} w-planes "
+            f"S {int(ob.supports.min())}-{int(ob.supports.max())}, oversample 8")
+
+
+_GCF_CACHE = {}
+
+
+def _gcf_host(ob):
+    """complex128 GCFs for the reference arm, from the numpy restatement of the
+    reference's generator (no engine code on that arm)."""
+    key = ob.name
+    if key in _GCF_CACHE:
+        return _GCF_CACHE[key]
+    from oracle import oracle as O
+    from rc_gb300 import gcf as Gm
+
+    tp = Gm.pswf_taper(ob.max_support)
+    out = np.concatenate([O.gcf_layers(w, int(S), ob.max_support, ob.scale / 2, taper=tp).ravel()
+                          for w, S in zip(ob.w_planes, ob.supports)])
+    _GCF_CACHE[key] = out
+    return out
+
+
+# ---------------------------------------------------------------- our arm
+def our_arm(args):
+    import torch
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    dev = torch.device("cuda", local)
+
+    from rc_gb300 import gcf as Gm
+    from rc_gb300 import lib as L
+    from rc_gb300.engine import Plan
+
+    L.load()
+    ob = load_workload(args.config)
+    # shard by replica: each rank grids its own observation of the same size
+    if world > 1 and rank > 0:
+        from rc_gb300 import synth
+
+        ob = synth.config(args.config, seed=synth.SEED0 + 1000 * rank)
+    G = ob.grid_size
+    s = torch.cuda.current_stream(dev)
+    tp = Gm.pswf_taper(ob.max_support)
+    t0 = time.perf_counter()
+    g64, g32, offs = Gm.generate(ob.w_planes, ob.supports, ob.max_support, ob.scale / 2, taper=tp,
+                                 device=dev)
+    torch.cuda.synchronize()
+    gcf_ms = 1e3 * (time.perf_counter() - t0)
+
+    d_uvw = torch.tensor(ob.uvw, device=dev)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    plan = Plan(d_uvw, scale=ob.scale, grid_size=G, grid_shape=(G, G), supports=ob.supports,
+                w_range=(ob.w_low, ob.w_high), tile=args.tile, threads=args.threads,
+                period_cap=args.cap)
+    torch.cuda.synchronize()
+    plan_ms = 1e3 * (time.perf_counter() - t0)
+    st = plan.stats()
+    kept, taps = st["kept"], st["taps"]
+
+    vis32 = torch.tensor(ob.vis, dtype=torch.complex64, device=dev)
+    vis64 = torch.tensor(ob.vis, dtype=torch.complex128, device=dev)
+    grid = torch.zeros((G, G), dtype=torch.complex64, device=dev)
+    pred = torch.empty(ob.n, dtype=torch.complex64, device=dev)
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=dev)
+
+    # model grid for degridding: the FP64 dirty grid of the observation
+    grid64 = torch.zeros((G, G), dtype=torch.complex128, device=dev)
+    plan.grid64(vis64, g64, grid64)
+    model32 = grid64.to(torch.complex64)
+    pred64 = plan.degrid64(g64, grid64)
+    torch.cuda.synchronize()
+
+    # accuracy of the FP32 pair against the plain FP64 path (itself pinned to
+    # the oracle at 1e-12 by the tests)
+    grid.zero_()
+    plan.grid(vis32, g32, grid)
+    plan.degrid(g32, model32, out=pred)
+    torch.cuda.synchronize()
+    err_grid = float(torch.linalg.vector_norm(grid.to(torch.complex128) - grid64) /
+                     torch.linalg.vector_norm(grid64))
+    err_deg = float(torch.linalg.vector_norm(pred.to(torch.complex128) - pred64) /
+                    torch.linalg.vector_norm(pred64))
+
+    def step():
+        grid.zero_()
+        plan.grid(vis32, g32, grid)
+        plan.degrid(g32, model32, out=pred)
+
+    # capture one step in a CUDA graph
+    use_graph = not args.no_graph
+    if use_graph:
+        side = torch.cuda.Stream(dev)
+        side.wait_stream(s)
+        with torch.cuda.stream(side):
+            step()
+        s.wait_stream(side)
+        torch.cuda.synchronize()
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph):
+            step()
+        run = graph.replay
+    else:
+        run = step
+
+    # per-kernel timing (eager, events on the launching stream)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    kg, kd = [], []
+    for i in range(args.warmup + args.steps):
+        flush.fill_(float(i))
+        grid.zero_()
+        ev[0].record(s)
+        plan.grid(vis32, g32, grid)
+        ev[1].record(s)
+        plan.degrid(g32, model32, out=pred)
+        ev[2].record(s)
+        ev[2].synchronize()
+        if i >= args.warmup:
+            kg.append(ev[0].elapsed_time(ev[1]))
+            kd.append(ev[1].elapsed_time(ev[2]))
+
+    # timed steps
+    for i in range(args.warmup):
+        flush.fill_(float(i))
+        run()
+    torch.cuda.synchronize()
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+    torch.cuda.synchronize()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    with ClockSampler(local) as clk:
+        wall0 = time.perf_counter()
+        for i in range(args.steps):
+            flush.fill_(float(i + 7))
+            starts[i].record(s)
+            run()
+            ends[i].record(s)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - wall0
+    step_ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
+    t_step = float(np.mean(step_ms))
+    if world > 1:
+        import torch.distributed as dist
+
+        tt = torch.tensor([t_step], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_step = float(tt.item())
+        dist.barrier()
+    value = world * ob.n / (t_step * 1e-3) / 1e6
+
+    # plain FP64 GPU path, same step
+    k64 = []
+    for i in range(2 + max(2, args.steps // 4)):
+        flush.fill_(float(i))
+        grid64.zero_()
+        ev[0].record(s)
+        plan.grid64(vis64, g64, grid64)
+        plan.degrid64(g64, grid64, out=pred64)
+        ev[1].record(s)
+        ev[1].synchronize()
+        if i >= 2:
+            k64.append(ev[0].elapsed_time(ev[1]))
+    fp64_mvis = ob.n / (np.mean(k64) * 1e-3) / 1e6
+
+    # roofline of the dominant kernel (algorithmic bytes, unfused per-tap model)
+    peak, peak_kind = measured_peaks()
+    bytes_grid = 32 * kept + 24 * taps
+    bytes_deg = 40 * kept + 16 * taps
+    tg, td = float(np.mean(kg)), float(np.mean(kd))
+    if tg >= td:
+        dom, b_dom, t_dom = "k_grid_tiled", bytes_grid, tg
+    else:
+        dom, b_dom, t_dom = "k_degrid_tiled", bytes_deg, td
+    achieved = b_dom / (t_dom * 1e-3) / 1e9
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tpath):
+        try:
+            traffic = json.load(open(tpath)).get(args.config, {}).get(dom)
+        except Exception:
+            traffic = None
+
+    # end to end through the public API: pinned host vis + model grid in,
+    # grid + predictions out, every step
+    h_vis = torch.tensor(ob.vis, dtype=torch.complex64).pin_memory()
+    h_model = model32.cpu().pin_memory()
+    h_grid = torch.empty((G, G), dtype=torch.complex64).pin_memory()
+    h_pred = torch.empty(ob.n, dtype=torch.complex64).pin_memory()
+    d_vis_e = torch.empty_like(vis32)
+    d_model_e = torch.empty_like(model32)
+    e2e = []
+    for i in range(args.warmup + args.steps):
+        flush.fill_(float(i))
+        ev[0].record(s)
+        d_vis_e.copy_(h_vis, non_blocking=True)
+        d_model_e.copy_(h_model, non_blocking=True)
+        grid.zero_()
+        plan.grid(d_vis_e, g32, grid)
+        plan.degrid(g32, d_model_e, out=pred)
+        h_grid.copy_(grid, non_blocking=True)
+        h_pred.copy_(pred, non_blocking=True)
+        ev[1].record(s)
+        ev[1].synchronize()
+        if i >= args.warmup:
+            e2e.append(ev[0].elapsed_time(ev[1]))
+    e2e_mvis = world * ob.n / (float(np.mean(e2e)) * 1e-3) / 1e6
+    h2d = h_vis.numel() * 8 + h_model.numel() * 8
+    d2h = h_grid.numel() * 8 + h_pred.numel() * 8
+
+    # CPU baseline (rank 0, N = 1 only): the oracle port on the host cores
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        offs_np, _ = Gm.layout(ob.supports)
+        n, dt, used, _, _ = cpu_leg(ob, ob.supports, g64.cpu().numpy(), offs_np, args.cpu_sample,
+                                    os.cpu_count() or 1)
+        cpu = {"value": round(n / dt / 1e6, 3), "unit": "Mvis/s", "cores": used, "kind": "port",
+               "sample": f"first {n} of {ob.n} visibilities, grid + degrid, FP64, "
+                         f"{used} threads, {dt:.1f} s"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(value, 3), "unit": "Mvis/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t_step, 4),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded); no public dataset",
+            "config": {"workload": _workload_desc(ob), "visibilities": ob.n, "kept": kept,
+                       "taps": taps, "grid": f"{G}x{G} complex64",
+                       "l2": "flushed (256 MiB write) before every step",
+                       "tile": st["tile"], "threads": st["threads"], "graph": use_graph,
+                       "parallelism": f"replicas x{world}"},
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1),
+                         "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
+                         "peak_kind": peak_kind, "traffic": traffic,
+                         "algorithmic_bytes_per_launch": int(b_dom)},
+            "kernels_ms": {"grid_f32": round(tg, 4), "degrid_f32": round(td, 4),
+                           "grid_frac_of_roofline": round(bytes_grid / (tg * 1e-3) / 1e9 / peak, 4),
+                           "degrid_frac_of_roofline": round(bytes_deg / (td * 1e-3) / 1e9 / peak, 4),
+                           "plan_ms": round(plan_ms, 2), "gcf_generate_ms": round(gcf_ms, 2)},
+            "fp64_plain": {"value": round(fp64_mvis, 3), "unit": "Mvis/s",
+                           "ms_per_step": round(float(np.mean(k64)), 3),
+                           "speedup_f32_over_f64": round(value / world / fp64_mvis, 2)},
+            "rel_l2_vs_fp64": {"grid": err_grid, "degrid": err_deg, "bar": 1e-5},
+            "e2e": {"value": round(e2e_mvis, 3), "unit": "Mvis/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "ms_per_step": round(float(np.mean(e2e)), 3)},
+            "cpu_baseline": cpu,
+            "clocks": clk.summary(),
+            "gpu_launches": 2 * args.steps,
+            "wall_s_timed_region": round(wall, 4),
+        }
+        print(json.dumps(line))
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+    return 0
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="c2")
+    ap.add_argument("--tile", type=int, default=0)
+    ap.add_argument("--threads", type=int, default=0)
+    ap.add_argument("--cap", type=int, default=0)
+    ap.add_argument("--no-graph", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-sample", type=int, default=1 << 20)
+    args = ap.parse_args(argv)
+    if args.warmup < 3 and args.impl == "ours":
+        args.warmup = 3
+    if args.impl == "reference":
+        return reference_arm(args)
+    return our_arm(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

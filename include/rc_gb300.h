@@ -1,0 +1,203 @@
+/*
+ * rc_gb300 — GB300-native w-projection gridding / degridding engine.
+ *
+ * C ABI of librc_gb300.so.  Two layers:
+ *
+ *  1. Drop-in symbols of the reference's kernel-binding ABI
+ *     (SKA-ScienceDataProcessor/RC, MS5/MS6 DNA/Flow `Flow.Halide`): the same
+ *     names, argument order, buffer_t layout and return conventions.  They take
+ *     HOST buffers, run on the GPU, and return only when the result is back in
+ *     host memory (the reference's semantics).
+ *
+ *  2. The engine API on DEVICE pointers (gb_*): a visibility plan (FP64 index
+ *     math, w-plane assignment, sort/bin by grid tile), the FP32 batched
+ *     gridder/degridder written as an exact adjoint pair, the plain FP64
+ *     gridder/degridder, and on-GPU w-kernel (GCF) generation.  Every launch
+ *     goes on the caller's stream and can be captured in a CUDA graph.
+ *
+ * Return value of every int function: 0 on success, negative on error;
+ * gb_last_error() gives the message of the calling thread's last error.
+ */
+#ifndef RC_GB300_H
+#define RC_GB300_H
+
+#include <stdbool.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ buffer_t
+ * Legacy Halide buffer descriptor, 72 bytes, byte-for-byte the layout the
+ * reference's Haskell marshaller writes (MS6/kernel/common/halide_buf.h:17-27;
+ * offsets 8/16/32/48/64/68 in MS6/dna/flow/Flow/Halide/BufferT.hs:26-99).
+ * `dev` is ignored (the reference never sets a device pointer,
+ * BufferT.hs:60-78); `host` is the data, `min` the coordinate of its first
+ * element in each dimension.  elem_size must be 8 (double). */
+#ifndef BUFFER_T_DEFINED
+#define BUFFER_T_DEFINED
+typedef struct buffer_t {
+  uint64_t dev;
+  uint8_t *host;
+  int32_t extent[4];
+  int32_t stride[4];
+  int32_t min[4];
+  int32_t elem_size;
+  bool host_dirty;
+  bool dev_dirty;
+  uint8_t _padding[10 - sizeof(void *)];
+} buffer_t;
+#endif
+
+/* ------------------------------------------------------------------ errors */
+#define GB_OK 0
+/* legacy "unsupported GCF size" codes of the reference dispatchers */
+#define GB_ERR_SCATTER_SIZE (-444)     /* MS6/kernel/cpu/gridding/scatter1.cpp:19 */
+#define GB_ERR_DEGRID_SIZE (-555)      /* MS6/kernel/cpu/gridding/degrid1.cpp:18 */
+#define GB_ERR_SCATTER_GPU_SIZE (-222) /* MS6/kernel/gpu/gridding/kern_scatter_gpu1.cpp:31 */
+#define GB_ERR_DEGRID_GPU_SIZE (-333)  /* MS6/kernel/gpu/gridding/kern_degrid_gpu1.cpp:71 */
+#define GB_ERR_ARG (-1001)      /* malformed buffer / argument */
+#define GB_ERR_CUDA (-1002)     /* CUDA runtime or cuFFT error */
+#define GB_ERR_TIMEOUT (-1003)  /* a bounded device-side wait ran out */
+#define GB_ERR_NOMEM (-1004)    /* device or host allocation failed */
+#define GB_ERR_CAPACITY (-1005) /* a size exceeds a documented limit */
+
+const char *gb_last_error(void);
+const char *gb_version(void);
+
+/* ------------------------------------------------------------------ layer 1: reference ABI
+ * Gridder type (Haskell, MS6/programs/Kernel/Gridder.hs:65-71):
+ *   HalideBind Double (HalideBind Int32 (HalideBind Int32
+ *     (HalideFun '[VisRepr, GCFsRepr] UVGMarginRepr)))
+ * vis: dims (5, N) stride (1, 5), fields u, v, w (wavelengths), re, im.
+ * gcf: dims (2, S, S, 64) strides (1, 2, 2S, 2S^2), phase index ou + 8*ov.
+ * uvg: dims (2, W, H) strides (1, 2, stride2), min (0, u0, v0): accumulated
+ *      in place (+=), never overwritten.
+ * The reference dispatchers accept S in {8, 16, 32, 64} and return the legacy
+ * code otherwise; these do the same (the engine below accepts any S). */
+
+/* replaces MS6/kernel/gpu/gridding/kern_scatter_gpu1.cpp:21-40 */
+int kern_scatter_gpu1(double scale, int32_t grid_size, int32_t margin_size,
+                      buffer_t *vis, buffer_t *gcf, buffer_t *uvg);
+/* replaces MS6/kernel/cpu/gridding/scatter1.cpp:9-20 (the CPU slot; runs on the GPU) */
+int kern_scatter(double scale, int32_t grid_size, int32_t margin_size,
+                 buffer_t *vis, buffer_t *gcf, buffer_t *uvg);
+/* replaces MS6/kernel/nvidia/gridder/halide_api.cu:4-29, in the form the
+ * Haskell side binds it (MS6/programs/Kernel/Gridder.hs:70: three scalars,
+ * margin included); same semantics as kern_scatter_gpu1. */
+int nvGridder(double scale, int32_t grid_size, int32_t margin_size,
+              buffer_t *vis, buffer_t *gcf, buffer_t *uvg);
+
+/* Degridder type (MS6/programs/Kernel/Degrid.hs:146-147): vis_out = vis
+ * minus sum(grid * gcf) for in-bound visibilities (no conjugate), u,v,w
+ * copied; uvg is the full grid, min 0.
+ * replaces MS6/kernel/gpu/gridding/kern_degrid_gpu1.cpp:61-81 */
+int kern_degrid_gpu1(double scale, int32_t grid_size, int32_t margin_size,
+                     buffer_t *gcf, buffer_t *uvg, buffer_t *vis, buffer_t *vis_out);
+/* replaces MS6/kernel/cpu/gridding/degrid1.cpp:9-19 */
+int kern_degrid(double scale, int32_t grid_size, int32_t margin_size,
+                buffer_t *gcf, buffer_t *uvg, buffer_t *vis, buffer_t *vis_out);
+
+/* replaces MS6/kernel/cpu/gridding/init.cpp:8-15 (zero a complex grid buffer) */
+int kern_init(buffer_t *uvg);
+/* replaces MS6/kernel/cpu/gridding/psf_vis.cpp:16-27 (vis_out = vis with re=1, im=0) */
+int kern_psf_vis(buffer_t *vis, buffer_t *vis_out);
+
+/* ------------------------------------------------------------------ layer 2: engine API */
+
+typedef struct gb_plan gb_plan;
+
+/* Geometry of one grid and its w-planes.  The grid is the full grid
+ * (min 0): ext_x * ext_y pixels, row pitch `pitch` complex elements.
+ * grid_size (the reference's centring parameter), scale (FoV in radians,
+ * the reference's `scale`), and margin (the reference's margin_size; pass the
+ * largest support to reproduce the MS6 bounds) follow the reference meaning.
+ * supports[p] is plane p's GCF support S_p (>= 1, <= GB_MAX_SUPPORT);
+ * gcf_offsets[p] is the offset, in complex elements, of plane p's GCF
+ * ([64][S_p][S_p], phase ou + 8*ov, row sy, column sx) inside the GCF array
+ * passed to the execute calls.  Planes are assigned per visibility by the
+ * reference's w-binning rule over [w_low, w_high] (Binning.hs:85-89), or
+ * taken from an explicit per-visibility plane array. */
+#define GB_MAX_SUPPORT 256
+#define GB_MAX_PLANES 4096
+typedef struct gb_geometry {
+  double scale;
+  int32_t grid_size;
+  int32_t margin;
+  int32_t ext_x, ext_y;
+  int64_t pitch;
+  int32_t n_planes;
+  int32_t tile;            /* grid tile edge of the FP32 kernels (8..128): 0 = 32 */
+  int32_t threads;         /* threads per CTA of the FP32 kernels (128, 256, 512): 0 = 256 */
+  int32_t period_cap;      /* largest footprint piece edge (8..64): 0 = 32 */
+  const int32_t *supports; /* host, n_planes */
+  const int64_t *gcf_offsets; /* host, n_planes */
+  double w_low, w_high;    /* w-binning range (ignored with an explicit plane array) */
+} gb_geometry;
+
+/* Build a plan for n_vis visibilities.  d_uvw: device, u v w doubles of
+ * visibility t at d_uvw[t*uvw_stride + {0,1,2}].  d_plane: optional device
+ * int32 plane index per visibility (negative = skip), else NULL.  The plan
+ * keeps d_uvw's address (for the plain FP64 path) but none of the visibility
+ * values; keep d_uvw alive while the plan is used.  Runs on `stream`
+ * (cudaStream_t) and synchronises it once. */
+int gb_plan_create(const gb_geometry *geo, int64_t n_vis, const double *d_uvw,
+                   int64_t uvw_stride, const int32_t *d_plane, void *stream,
+                   gb_plan **out);
+int gb_plan_destroy(gb_plan *plan);
+
+/* Statistics of a plan: [0] visibilities kept, [1] sum over kept visibilities
+ * of S_v^2 (taps), [2] work items, [3] grid tiles with work, [4] tile edge,
+ * [5] largest support, [6] threads per CTA. */
+int gb_plan_stats(const gb_plan *plan, int64_t *stats7);
+
+/* Per-visibility index record (x0, y0, phase ou+8*ov, plane, kept) as the
+ * plan computed it, 5 int32 per visibility, into device memory. */
+int gb_plan_export_index(const gb_plan *plan, int32_t *d_out5, void *stream);
+
+/* FP32 batched adjoint pair (complex64, interleaved re/im floats).
+ *   G (gridding):   grid[pix] += sum_v vis[v] * gcf_v[pix - corner_v]
+ *   D (degridding): pred[v]    = sum_pix grid[pix] * conj(gcf_v[pix - corner_v])
+ * D is the exact adjoint of G: <D x, y> = <x, G y>.  mode 1 of the degridder
+ * gives the reference's kern_degrid product instead: pred = -sum grid * gcf.
+ * Visibilities the plan skipped get pred = 0.  Per-tile partial sums are
+ * compensated (error-free transformation) in shared memory. */
+int gb_grid_f32(gb_plan *plan, const float *d_vis, const float *d_gcf, float *d_grid,
+                void *stream);
+int gb_degrid_f32(gb_plan *plan, const float *d_gcf, const float *d_grid, float *d_pred,
+                  int32_t mode, void *stream);
+/* Forward / backward names of the pair: degrid forward = D, its backward
+ * (vector-Jacobian product) = G; grid forward = G, backward = D. */
+int gb_degrid_forward(gb_plan *plan, const float *d_gcf, const float *d_grid,
+                      float *d_pred, void *stream);
+int gb_degrid_backward(gb_plan *plan, const float *d_gcf, const float *d_pred_grad,
+                       float *d_grid_grad, void *stream);
+
+/* Plain FP64 path (complex128): no tiling, no sorting; one warp per
+ * visibility, FP64 atomics into the grid.  Same operators as above. */
+int gb_grid_f64(gb_plan *plan, const double *d_vis, const double *d_gcf, double *d_grid,
+                void *stream);
+int gb_degrid_f64(gb_plan *plan, const double *d_gcf, const double *d_grid,
+                  double *d_pred, int32_t mode, void *stream);
+
+/* On-GPU w-kernel generation (MS4/kernel/cpu/gcf/GCF.cpp semantics): for
+ * each plane p, the FP64 phase screen exp(-2 pi i w_p (1 - sqrt(1-l^2-m^2)))
+ * times taper(l) taper(m) on a max_support^2 patch (l, m = k * t2 /
+ * (max_support/2)), centred in an (8 max_support)^2 arena, centred inverse
+ * FFT (cuFFT, FP64), per-phase normalisation by the sum of real parts, and
+ * extraction of the centred S_p x S_p taps per phase.  Writes complex128
+ * (d_gcf64, may be NULL) and complex64 (d_gcf32, may be NULL) GCF arrays laid
+ * out by gcf_offsets.  d_taper: device, max_support doubles, or NULL for none.
+ * Allocates its FFT workspace per call. */
+int gb_gcf_generate(int32_t n_planes, const double *w_planes, const int32_t *supports,
+                    const int64_t *gcf_offsets, int32_t max_support, double t2,
+                    const double *d_taper, double *d_gcf64, float *d_gcf32, void *stream);
+
+/* Zero `n_complex` complex64 grid elements (device). */
+int gb_grid_zero_f32(float *d_grid, int64_t n_complex, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RC_GB300_H */

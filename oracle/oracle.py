@@ -1,0 +1,281 @@
+"""ORACLE — test infrastructure only.
+
+Python face of the CPU FP64 restatement of the reference's gridding path.  Only
+tests/, __graft_entry__.smoke() and bench.py's cpu_baseline / reference legs
+may import this module, and only as the checker (or the timed CPU baseline);
+the rc_gb300 product never does.
+
+Contents
+  * ctypes bindings of oracle/gridref.c (kern_scatter / kern_degrid semantics,
+    multi-plane forms, w-binning);
+  * gcf_layers(): numpy restatement of the reference's w-kernel generator,
+    MS4/kernel/cpu/gcf/GCF.cpp:58-117 (screen, centred FFT) and :16-52
+    (per-phase normalisation, extraction), with FFTW's backward transform
+    (MS4/kernel/cpu/fft/fft_dyn_padded.cpp:76-103: fftshift, unnormalised
+    exp(+2*pi*i) DFT, fftshift) written as numpy's ifft2 times N^2;
+  * binsizer(): the w-range rule of MS6/programs/Kernel/Binning.hs:51-60;
+  * ms4_* wrappers of the reference's own compiled MS4 gridder/degridder
+    (oracle/_ref, built from the reference sources by `make -C oracle ref`),
+    used to pin the restatement where the two index conventions coincide.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+OVER = 8
+
+_lib = None
+_ms4 = None
+
+_i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+_i64p = np.ctypeslib.ndpointer(np.int64, flags="C_CONTIGUOUS")
+_f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+_i32, _i64, _f64 = C.c_int32, C.c_int64, C.c_double
+
+
+def build(ref: bool = True) -> None:
+    """Compile oracle/liboracle.so (and oracle/_ref when the reference is present)."""
+    subprocess.run(["make", "-s", "-C", HERE, "liboracle.so"], check=True)
+    if ref and os.path.isdir("/root/reference/MS4"):
+        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = os.path.join(HERE, "liboracle.so")
+        if not os.path.exists(path):
+            build(ref=False)
+        L = C.CDLL(path)
+        L.orc_index.argtypes = [_i64, _f64p, _i64, _f64, _i32, _i32, _i32, _i32, _i32, _i32, _i32, _i32p]
+        L.orc_scatter.argtypes = [_f64, _i32, _i32, _i32, _i64, _f64p, _i64, _f64p, _f64p,
+                                  _i32, _i32, _i32, _i32, _i64]
+        L.orc_degrid.argtypes = [_f64, _i32, _i32, _i32, _i64, _f64p, _i64, _f64p, _f64p,
+                                 _i32, _i32, _i32, _i32, _i64, _f64p, _i64]
+        L.orc_scatter_planes.argtypes = [_f64, _i32, _i32, _i64, _f64p, _i64, _f64p, _i32p, _i32p,
+                                         _i64p, _f64p, _f64p, _i32, _i32, _i64]
+        L.orc_scatter_planes_omp.argtypes = L.orc_scatter_planes.argtypes + [C.c_int]
+        L.orc_scatter_planes_omp.restype = C.c_int
+        L.orc_degrid_planes.argtypes = [_f64, _i32, _i32, _i64, _f64p, _i64, _i32p, _i32p, _i64p,
+                                        _f64p, _f64p, _i32, _i32, _i64, _i32, _f64p, C.c_int]
+        L.orc_wbin.argtypes = [_i64, _f64p, _i64, _f64, _f64, _i32, _i32p]
+        _lib = L
+    return _lib
+
+
+def _c(a, dt):
+    return np.ascontiguousarray(a, dtype=dt)
+
+
+# ---------------------------------------------------------------- single GCF (ABI form)
+def index(vis5, scale, grid_size, S, margin, min_x=0, min_y=0, ext_x=None, ext_y=None):
+    """(N,5) int32: x0, y0, ou, ov, in-bound — scatter.cpp:56-76."""
+    vis5 = _c(vis5, np.float64)
+    n = vis5.shape[0]
+    out = np.zeros((n, 5), np.int32)
+    lib().orc_index(n, vis5.reshape(-1), 5, scale, grid_size, S, margin, min_x, min_y,
+                    ext_x, ext_y, out.reshape(-1))
+    return out
+
+
+def scatter(scale, grid_size, margin, vis5, gcf, grid, min_x=0, min_y=0):
+    """kern_scatter semantics, in place on `grid` (complex128 [ext_y][ext_x])."""
+    vis5 = _c(vis5, np.float64)
+    S = gcf.shape[-1]
+    g = _c(gcf, np.complex128).view(np.float64).reshape(-1)
+    ext_y, ext_x = grid.shape
+    assert grid.dtype == np.complex128 and grid.flags.c_contiguous
+    lib().orc_scatter(scale, grid_size, margin, S, vis5.shape[0], vis5.reshape(-1), 5, g,
+                      grid.view(np.float64).reshape(-1), min_x, min_y, ext_x, ext_y, ext_x)
+    return grid
+
+
+def degrid(scale, grid_size, margin, gcf, grid, vis5, min_x=0, min_y=0):
+    """kern_degrid semantics: returns vis_out (N,5)."""
+    vis5 = _c(vis5, np.float64)
+    S = gcf.shape[-1]
+    g = _c(gcf, np.complex128).view(np.float64).reshape(-1)
+    grid = _c(grid, np.complex128)
+    ext_y, ext_x = grid.shape
+    out = np.zeros_like(vis5)
+    lib().orc_degrid(scale, grid_size, margin, S, vis5.shape[0], vis5.reshape(-1), 5, g,
+                     grid.view(np.float64).reshape(-1), min_x, min_y, ext_x, ext_y, ext_x,
+                     out.reshape(-1), 5)
+    return out
+
+
+# ---------------------------------------------------------------- multi-plane (engine form)
+def scatter_planes(scale, grid_size, margin, uvw, vis, plane, supports, gcf_flat, gcf_off,
+                   grid, nthreads=1):
+    """grid += G(vis) over all planes.  vis complex128 (N,), gcf_flat complex128."""
+    uvw = _c(uvw, np.float64)
+    vis = _c(vis, np.complex128)
+    ext_y, ext_x = grid.shape
+    args = (scale, grid_size, margin, uvw.shape[0], uvw.reshape(-1), uvw.shape[1],
+            vis.view(np.float64), _c(plane, np.int32), _c(supports, np.int32),
+            _c(gcf_off, np.int64), _c(gcf_flat, np.complex128).view(np.float64),
+            grid.view(np.float64).reshape(-1), ext_x, ext_y, ext_x)
+    if nthreads == 1:
+        lib().orc_scatter_planes(*args)
+        return 1
+    return lib().orc_scatter_planes_omp(*args, nthreads)
+
+
+def degrid_planes(scale, grid_size, margin, uvw, plane, supports, gcf_flat, gcf_off, grid,
+                  mode=0, nthreads=1):
+    """Predicted visibilities (complex128 (N,)).  mode 0: exact adjoint (conj GCF);
+    mode 1: the reference kern_degrid product with its sign (-sum grid*gcf)."""
+    uvw = _c(uvw, np.float64)
+    grid = _c(grid, np.complex128)
+    ext_y, ext_x = grid.shape
+    pred = np.zeros(uvw.shape[0], np.complex128)
+    lib().orc_degrid_planes(scale, grid_size, margin, uvw.shape[0], uvw.reshape(-1),
+                            uvw.shape[1], _c(plane, np.int32), _c(supports, np.int32),
+                            _c(gcf_off, np.int64), _c(gcf_flat, np.complex128).view(np.float64),
+                            grid.view(np.float64).reshape(-1), ext_x, ext_y, ext_x, mode,
+                            pred.view(np.float64), nthreads)
+    return pred
+
+
+def wbin(uvw, low, high, bins):
+    uvw = _c(uvw, np.float64)
+    out = np.zeros(uvw.shape[0], np.int32)
+    lib().orc_wbin(uvw.shape[0], uvw.reshape(-1), uvw.shape[1], low, high, bins, out)
+    return out
+
+
+def binsizer(w):
+    """Binning.hs:51-60: low = min(0, min w), high0 = max(0, max w) (the fold starts
+    at (0,0)), high = high0 + (high0-low)*1e-4."""
+    low = min(0.0, float(np.min(w))) if len(w) else 0.0
+    high0 = max(0.0, float(np.max(w))) if len(w) else 0.0
+    return low, high0 + (high0 - low) * 0.0001
+
+
+# ---------------------------------------------------------------- GCF generation (MS4 spec)
+def gcf_layers(w, support, max_support, t2, taper=None, over=OVER):
+    """One w-plane's oversampled GCF in the MS6 layout [ou + 8*ov][sy][sx] (complex128).
+
+    GCF.cpp:58-117: screen (cos 2*pi*ph, -sin 2*pi*ph), ph = w*(1-sqrt(1-x^2-y^2)),
+    x = i*t2/(max_support/2) on rows, y = j*t2/(max_support/2) on columns, for
+    i, j in [-r, r + max_support%2); centred in a (over*max_support)^2 zero arena;
+    centred backward FFT; per-phase sums of real parts over the whole arena
+    (GCF.cpp:25-32); centred support x support extraction (GCF.cpp:39-51).
+    `taper` (optional, length max_support) multiplies the screen separably; the
+    reference screen has none.
+    """
+    size = max_support * over
+    r = max_support // 2
+    i = np.arange(-r, r + max_support % 2, dtype=np.float64)
+    x = i * (t2 / float(r))
+    X = x[:, None]
+    Y = x[None, :]
+    ph = w * (1.0 - np.sqrt(1.0 - X * X - Y * Y))
+    screen = np.cos(2.0 * np.pi * ph) - 1j * np.sin(2.0 * np.pi * ph)
+    if taper is not None:
+        t = np.asarray(taper, np.float64)
+        screen = screen * (t[:, None] * t[None, :])
+    arena = np.zeros((size, size), np.complex128)
+    a0 = size // 2 - r
+    arena[a0:a0 + max_support, a0:a0 + max_support] = screen
+    arena = np.fft.fftshift(np.fft.ifft2(np.fft.fftshift(arena))) * float(size * size)
+    a4 = arena.reshape(max_support, over, max_support, over)  # [su][ou][sv][ov]
+    sums = a4.real.sum(axis=(0, 2))  # [ou][ov]
+    c = max_support // 2 - support // 2
+    sub = a4[c:c + support, :, c:c + support, :]  # [su][ou][sv][ov]
+    ms4 = sub.transpose(1, 3, 0, 2) / sums[:, :, None, None]  # [ou][ov][su][sv]
+    # MS6 layout: [ov][ou][sy=sv][sx=su] flattened as phase ou + 8*ov
+    return np.ascontiguousarray(ms4.transpose(1, 0, 3, 2)).reshape(over * over, support, support)
+
+
+# ---------------------------------------------------------------- reference MS4 binary (pinning)
+def _aligned_zeros(shape, dtype, align=64):
+    """Zeroed array whose data starts on an `align`-byte boundary (the MS4 code
+    uses aligned AVX loads/stores on the grid)."""
+    dt = np.dtype(dtype)
+    n = int(np.prod(shape)) * dt.itemsize
+    raw = np.zeros(n + align, np.uint8)
+    off = (-raw.ctypes.data) % align
+    return raw[off:off + n].view(dt).reshape(shape)
+
+
+def ms4_available():
+    return os.path.exists(os.path.join(HERE, "_ref", "libms4ref.so"))
+
+
+def ms4():
+    global _ms4
+    if _ms4 is None:
+        L = C.CDLL(os.path.join(HERE, "_ref", "libms4ref.so"))
+        sig = [_f64, _f64, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+               C.c_int, C.c_int, C.c_int, C.c_void_p]
+        L.gridKernelCPUFullGCF.argtypes = sig
+        L.gridKernelCPUFullGCF.restype = C.c_ulonglong
+        L.deGridKernelCPUFullGCF.argtypes = sig
+        L.deGridKernelCPUFullGCF.restype = C.c_ulonglong
+        _ms4 = L
+    return _ms4
+
+
+def _ms4_args(scale, uvw_bl, vis_bl, layers_ms4, supp, grid_size):
+    """Pointer tables for the MS4 calling convention, one w-plane (index 0)."""
+    nbl, ts = uvw_bl.shape[:2]
+    keep = []
+    uvw_ptrs = (C.c_void_p * nbl)()
+    vis_ptrs = (C.c_void_p * nbl)()
+    for b in range(nbl):
+        u = np.ascontiguousarray(uvw_bl[b], np.float64)
+        v = np.ascontiguousarray(vis_bl[b], np.complex128)
+        keep += [u, v]
+        uvw_ptrs[b] = u.ctypes.data
+        vis_ptrs[b] = v.ctypes.data
+    lay = np.ascontiguousarray(layers_ms4, np.complex128)  # [ou][ov][su][sv]
+    keep.append(lay)
+    gptrs = (C.c_void_p * (OVER * OVER))()
+    for k in range(OVER * OVER):
+        gptrs[k] = lay.ctypes.data + k * supp * supp * 16
+    bl_supps = np.full(nbl, supp, np.int32)
+    gcf_supps = np.array([supp], np.int32)
+    keep += [bl_supps, gcf_supps]
+    return keep, uvw_ptrs, vis_ptrs, gptrs, bl_supps, gcf_supps
+
+
+def ms4_grid(scale, uvw_bl, vis_bl, gcf_ms6, grid_size):
+    """Reference MS4 gridKernelCPUFullGCF on one w-plane; returns the grid in the
+    MS6 orientation [v][u] (complex128 grid_size^2)."""
+    supp = gcf_ms6.shape[-1]
+    layers = gcf_ms6.reshape(OVER, OVER, supp, supp).transpose(1, 0, 3, 2)  # -> [ou][ov][su][sv]
+    keep, up, vp, gp, bls, gss = _ms4_args(scale, uvw_bl, vis_bl, layers, supp, grid_size)
+    grid = _aligned_zeros((grid_size, grid_size), np.complex128)  # [u][v]
+    ms4().gridKernelCPUFullGCF(scale, 1e300, uvw_bl.shape[0], bls.ctypes.data, grid.ctypes.data,
+                               C.cast(gp, C.c_void_p), C.cast(up, C.c_void_p),
+                               C.cast(vp, C.c_void_p), uvw_bl.shape[1], grid_size, grid_size,
+                               gss.ctypes.data)
+    del keep
+    return np.ascontiguousarray(grid.T)
+
+
+def ms4_degrid(scale, uvw_bl, grid_ms6, gcf_ms6):
+    """Reference MS4 deGridKernelCPUFullGCF on one w-plane: sum grid*gcf per
+    visibility (no conjugate).  grid_ms6 is [v][u]; returns (nbl, ts) complex128."""
+    supp = gcf_ms6.shape[-1]
+    grid_size = grid_ms6.shape[0]
+    layers = gcf_ms6.reshape(OVER, OVER, supp, supp).transpose(1, 0, 3, 2)
+    out = np.zeros(uvw_bl.shape[:2], np.complex128)
+    keep, up, vp, gp, bls, gss = _ms4_args(scale, uvw_bl, out, layers, supp, grid_size)
+    # the degridder writes through the visibility pointer table: point it at `out`
+    for b in range(uvw_bl.shape[0]):
+        vp[b] = out.ctypes.data + b * uvw_bl.shape[1] * 16
+    g = _aligned_zeros((grid_size, grid_size), np.complex128)
+    g[...] = grid_ms6.T  # -> [u][v]
+    ms4().deGridKernelCPUFullGCF(scale, 1e300, uvw_bl.shape[0], bls.ctypes.data, g.ctypes.data,
+                                 C.cast(gp, C.c_void_p), C.cast(up, C.c_void_p),
+                                 C.cast(vp, C.c_void_p), uvw_bl.shape[1], grid_size, grid_size,
+                                 gss.ctypes.data)
+    del keep
+    return out

@@ -1,0 +1,545 @@
+// Visibility plan: w-plane assignment, FP64 index math, and the sort / bin of
+// footprint pieces by (grid tile, period) that feeds the FP32 tiled kernels.
+//
+// It replaces the reference's host-side binning (MS6/programs/Kernel/
+// Binning.hs:34-181, a scalar Haskell pass per visibility) and the NVIDIA
+// gridder's host std::sort (MS6/kernel/nvidia/gridder/binsort.cpp:6-35) with
+// a counting sort on the GPU:
+//   1. k_plan_count: per visibility, plane + index math (FP64), then a
+//      histogram of pieces per (tile, period rank);
+//   2. host: exclusive scan of the histogram, work items (record ranges of
+//      one tile and one thread-group class, cut by a cost model), bundles of
+//      items for the persistent kernels, longest first;
+//   3. k_plan_fill: recompute the index, scatter 16-byte records into their
+//      bins.
+#include <algorithm>
+#include <cstdlib>
+#include <cstring>
+#include <numeric>
+#include <vector>
+
+#include "gb_common.cuh"
+#include "gb_plan.cuh"
+#include "gb_runtime.cuh"
+
+namespace gb {
+
+__global__ void k_plan_count(PlanDev P, const PlaneInfo* __restrict__ pl,
+                             const int32_t* __restrict__ plane_in, int32_t* __restrict__ plane_out,
+                             int32_t n_planes, double w_lo, double w_hi, int32_t T, int32_t ntx,
+                             int32_t nper, int32_t* __restrict__ hist,
+                             unsigned long long* __restrict__ counters) {
+  __shared__ unsigned long long s_kept, s_taps, s_recs;
+  if (threadIdx.x == 0) s_kept = s_taps = s_recs = 0ull;
+  __syncthreads();
+  unsigned long long kept = 0, taps = 0, recs = 0;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < P.n_vis;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const double* r = P.uvw + t * P.uvw_stride;
+    int32_t p = plane_in ? plane_in[t] : w_plane(r[2], w_lo, w_hi, n_planes);
+    if (p >= n_planes) p = -1;
+    plane_out[t] = p;
+    if (p < 0) continue;
+    const PlaneInfo q = pl[p];
+    const VisIndex ix =
+        vis_index(r[0], r[1], P.scale, P.grid_size, q.S, P.margin, 0, 0, P.ext_x, P.ext_y);
+    if (!ix.keep) continue;
+    kept++;
+    taps += (unsigned long long)q.S * q.S;
+    for (int ky = 0; ky < q.k; ky++) {
+      const int Y0 = ix.y0 + ky * q.P;
+      if (ky * q.P >= q.S) break;
+      for (int kx = 0; kx < q.k; kx++) {
+        if (kx * q.P >= q.S) break;
+        const int X0 = ix.x0 + kx * q.P;
+        const int64_t tile = (int64_t)(Y0 / T) * ntx + (X0 / T);
+        atomicAdd(&hist[tile * nper + q.rank], 1);
+        recs++;
+      }
+    }
+  }
+  atomicAdd(&s_kept, kept);
+  atomicAdd(&s_taps, taps);
+  atomicAdd(&s_recs, recs);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    atomicAdd(&counters[0], s_kept);
+    atomicAdd(&counters[1], s_taps);
+    atomicAdd(&counters[2], s_recs);
+  }
+}
+
+__global__ void k_plan_fill(PlanDev P, const PlaneInfo* __restrict__ pl, int32_t T, int32_t ntx,
+                            int32_t nper, const int32_t* __restrict__ offs,
+                            int32_t* __restrict__ cursor, Rec* __restrict__ recs) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < P.n_vis;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t p = P.plane[t];
+    if (p < 0) continue;
+    const PlaneInfo q = pl[p];
+    const double* r = P.uvw + t * P.uvw_stride;
+    const VisIndex ix =
+        vis_index(r[0], r[1], P.scale, P.grid_size, q.S, P.margin, 0, 0, P.ext_x, P.ext_y);
+    if (!ix.keep) continue;
+    const int64_t gbase = q.gcf_off + (int64_t)ix.phase * q.S * q.S;
+    for (int ky = 0; ky < q.k; ky++) {
+      const int oy = ky * q.P;
+      if (oy >= q.S) break;
+      const int Y0 = ix.y0 + oy;
+      const int wy = min(q.P, q.S - oy);
+      for (int kx = 0; kx < q.k; kx++) {
+        const int ox = kx * q.P;
+        if (ox >= q.S) break;
+        const int X0 = ix.x0 + ox;
+        const int wx = min(q.P, q.S - ox);
+        const int tx = X0 / T, ty = Y0 / T;
+        const int64_t key = ((int64_t)ty * ntx + tx) * nper + q.rank;
+        const int32_t pos = offs[key] + atomicAdd(&cursor[key], 1);
+        Rec rc;
+        rc.vis = (int32_t)t;
+        rc.gcf = (uint32_t)(gbase + (int64_t)oy * q.S + ox);
+        rc.xl = (uint8_t)(X0 - tx * T);
+        rc.yl = (uint8_t)(Y0 - ty * T);
+        rc.wx = (uint8_t)wx;
+        rc.wy = (uint8_t)wy;
+        rc.xm = (uint8_t)(X0 % q.P);
+        rc.ym = (uint8_t)(Y0 % q.P);
+        rc.pm1 = (uint8_t)(q.P - 1);
+        rc.sm1 = (uint8_t)(q.S - 1);
+        recs[pos] = rc;
+      }
+    }
+  }
+}
+
+__global__ void k_plan_export(PlanDev P, const int32_t* __restrict__ supports,
+                              int32_t* __restrict__ out5) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < P.n_vis;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t p = P.plane[t];
+    int32_t* o = out5 + 5 * t;
+    if (p < 0) {
+      o[0] = o[1] = o[2] = 0;
+      o[3] = p;
+      o[4] = 0;
+      continue;
+    }
+    const double* r = P.uvw + t * P.uvw_stride;
+    const VisIndex ix = vis_index(r[0], r[1], P.scale, P.grid_size, supports[p], P.margin, 0, 0,
+                                  P.ext_x, P.ext_y);
+    o[0] = ix.x0;
+    o[1] = ix.y0;
+    o[2] = ix.phase;
+    o[3] = p;
+    o[4] = ix.keep ? 1 : 0;
+  }
+}
+
+// Thread-group width for a period: the smallest power of two L >= 64 (and
+// <= NT) holding P^2 taps in at most two rounds; NT otherwise.
+static int class_width(int P, int NT) {
+  for (int L = 64; L <= NT; L *= 2)
+    if (P * P <= 2 * L) return L;
+  return NT;
+}
+
+static int blocks_for(int64_t n, int threads) {
+  int64_t b = (n + threads - 1) / threads;
+  const int64_t cap = (int64_t)sm_count() * 32;
+  if (b > cap) b = cap;
+  return (int)(b < 1 ? 1 : b);
+}
+
+static void free_plan(gb_plan* p) {
+  if (!p) return;
+  cudaFree(p->d_plane);
+  cudaFree(p->d_supports);
+  cudaFree(p->d_offsets);
+  cudaFree(p->d_planes);
+  cudaFree(p->d_recs);
+  cudaFree(p->d_items);
+  cudaFree(p->d_bundles);
+  cudaFree(p->d_queue);
+  delete p;
+}
+
+template <class T>
+static int dalloc(T** p, size_t n) {
+  cudaError_t e = cudaMalloc((void**)p, sizeof(T) * (n ? n : 1));
+  if (e != cudaSuccess) {
+    *p = nullptr;
+    gb_set_error(GB_ERR_NOMEM, "cudaMalloc(%zu): %s", sizeof(T) * n, cudaGetErrorString(e));
+    return GB_ERR_NOMEM;
+  }
+  return GB_OK;
+}
+
+struct HostItem {
+  Item it;
+  double cost;
+};
+
+static int build_plan(gb_plan* P, const gb_geometry* geo, int64_t n_vis, const double* d_uvw,
+                      int64_t uvw_stride, const int32_t* d_plane_in, cudaStream_t s) {
+  int rc;
+  const int np = geo->n_planes;
+  // ---- per-plane pieces, periods, classes
+  P->planes.resize(np);
+  std::vector<int> periods;
+  for (int p = 0; p < np; p++) {
+    PlaneInfo& q = P->planes[p];
+    q.S = geo->supports[p];
+    q.k = (q.S + P->pcap - 1) / P->pcap;
+    q.P = (q.S + q.k - 1) / q.k;
+    q.gcf_off = geo->gcf_offsets[p];
+    periods.push_back(q.P);
+    if (q.gcf_off + (int64_t)GB_PHASES * q.S * q.S > (int64_t)UINT32_MAX) {
+      gb_set_error(GB_ERR_CAPACITY, "GCF array exceeds 2^32 complex elements");
+      return GB_ERR_CAPACITY;
+    }
+  }
+  std::sort(periods.begin(), periods.end());
+  periods.erase(std::unique(periods.begin(), periods.end()), periods.end());
+  const int nper = (int)periods.size();
+  for (auto& q : P->planes)
+    q.rank = (int)(std::lower_bound(periods.begin(), periods.end(), q.P) - periods.begin());
+  // classes by group width, ascending
+  std::vector<int> widths;
+  for (int pp : periods) widths.push_back(class_width(pp, P->NT));
+  std::vector<int> cls_w = widths;
+  std::sort(cls_w.begin(), cls_w.end());
+  cls_w.erase(std::unique(cls_w.begin(), cls_w.end()), cls_w.end());
+  P->n_classes = (int)cls_w.size();
+  if (P->n_classes > kMaxClasses) {
+    gb_set_error(GB_ERR_CAPACITY, "too many thread-group classes");
+    return GB_ERR_CAPACITY;
+  }
+  std::vector<int> rank_cls(nper);
+  for (int r = 0; r < nper; r++)
+    rank_cls[r] = (int)(std::lower_bound(cls_w.begin(), cls_w.end(), widths[r]) - cls_w.begin());
+  const int smem_cap = tiled_max_smem();
+  for (int c = 0; c < P->n_classes; c++) {
+    ClassInfo& ci = P->cls[c];
+    ci.L = cls_w[c];
+    ci.pmax = 0;
+    for (int r = 0; r < nper; r++)
+      if (rank_cls[r] == c) ci.pmax = std::max(ci.pmax, periods[r]);
+    ci.A = P->T + ci.pmax - 1;
+    const size_t per_group = (size_t)ci.A * ci.A * 16 + (size_t)ci.L * 24;
+    int G = P->NT / ci.L;
+    while (G > 0 && (size_t)G * per_group > (size_t)smem_cap) G--;
+    if (G == 0) {
+      gb_set_error(GB_ERR_CAPACITY,
+                   "tile %d with period %d needs %zu B of shared memory (limit %d)", P->T,
+                   ci.pmax, per_group, smem_cap);
+      return GB_ERR_CAPACITY;
+    }
+    ci.G = G;
+  }
+  P->smem_grid = tiled_smem_grid(P->cls, P->n_classes, P->NT);
+  P->smem_degrid = tiled_smem_degrid(P->cls, P->n_classes, P->NT);
+  P->ctas_per_sm_grid = tiled_ctas_per_sm(P, true);
+  P->ctas_per_sm_degrid = tiled_ctas_per_sm(P, false);
+
+  // ---- device tables
+  if ((rc = dalloc(&P->d_plane, n_vis)) || (rc = dalloc(&P->d_supports, np)) ||
+      (rc = dalloc(&P->d_offsets, np)) || (rc = dalloc(&P->d_planes, np)) ||
+      (rc = dalloc(&P->d_queue, 2)))
+    return rc;
+  GB_CUDA_TRY(cudaMemcpyAsync(P->d_supports, geo->supports, sizeof(int32_t) * np,
+                              cudaMemcpyHostToDevice, s));
+  GB_CUDA_TRY(cudaMemcpyAsync(P->d_offsets, geo->gcf_offsets, sizeof(int64_t) * np,
+                              cudaMemcpyHostToDevice, s));
+  GB_CUDA_TRY(cudaMemcpyAsync(P->d_planes, P->planes.data(), sizeof(PlaneInfo) * np,
+                              cudaMemcpyHostToDevice, s));
+  PlanDev& D = P->dev;
+  D.n_vis = n_vis;
+  D.uvw = d_uvw;
+  D.uvw_stride = uvw_stride;
+  D.plane = P->d_plane;
+  D.supports = P->d_supports;
+  D.gcf_offsets = P->d_offsets;
+  D.scale = geo->scale;
+  D.grid_size = geo->grid_size;
+  D.margin = geo->margin;
+  D.ext_x = geo->ext_x;
+  D.ext_y = geo->ext_y;
+  D.pitch = geo->pitch;
+
+  // ---- histogram
+  P->ntx = (geo->ext_x + P->T - 1) / P->T;
+  P->nty = (geo->ext_y + P->T - 1) / P->T;
+  const int64_t nkeys = (int64_t)P->ntx * P->nty * nper;
+  if (nkeys >= (int64_t)INT32_MAX) {
+    gb_set_error(GB_ERR_CAPACITY, "too many (tile, period) bins");
+    return GB_ERR_CAPACITY;
+  }
+  int32_t *d_hist = nullptr, *d_offs = nullptr;
+  unsigned long long* d_cnt = nullptr;
+  if ((rc = dalloc(&d_hist, nkeys)) || (rc = dalloc(&d_offs, nkeys + 1)) ||
+      (rc = dalloc(&d_cnt, 3))) {
+    cudaFree(d_hist);
+    cudaFree(d_offs);
+    cudaFree(d_cnt);
+    return rc;
+  }
+  struct Tmp {
+    void* p[3];
+    ~Tmp() {
+      for (void* q : p) cudaFree(q);
+    }
+  } tmp{{d_hist, d_offs, d_cnt}};
+  GB_CUDA_TRY(cudaMemsetAsync(d_hist, 0, sizeof(int32_t) * nkeys, s));
+  GB_CUDA_TRY(cudaMemsetAsync(d_cnt, 0, sizeof(unsigned long long) * 3, s));
+  if (n_vis > 0) {
+    k_plan_count<<<blocks_for(n_vis, 256), 256, 0, s>>>(
+        D, P->d_planes, d_plane_in, P->d_plane, np, geo->w_low, geo->w_high, P->T, P->ntx, nper,
+        d_hist, d_cnt);
+    GB_CUDA_TRY(cudaGetLastError());
+  }
+  std::vector<int32_t> hist(nkeys);
+  unsigned long long cnt[3];
+  GB_CUDA_TRY(cudaMemcpyAsync(hist.data(), d_hist, sizeof(int32_t) * nkeys, cudaMemcpyDeviceToHost,
+                              s));
+  GB_CUDA_TRY(cudaMemcpyAsync(cnt, d_cnt, sizeof(cnt), cudaMemcpyDeviceToHost, s));
+  GB_CUDA_TRY(cudaStreamSynchronize(s));
+  P->kept = (int64_t)cnt[0];
+  P->taps = (int64_t)cnt[1];
+  P->n_recs = (int64_t)cnt[2];
+  if (P->n_recs >= (int64_t)INT32_MAX) {
+    gb_set_error(GB_ERR_CAPACITY, "more than 2^31 footprint pieces");
+    return GB_ERR_CAPACITY;
+  }
+
+  // ---- scan + items
+  std::vector<int32_t> offs(nkeys + 1);
+  int64_t acc = 0;
+  for (int64_t k = 0; k < nkeys; k++) {
+    offs[k] = (int32_t)acc;
+    acc += hist[k];
+  }
+  offs[nkeys] = (int32_t)acc;
+
+  // cost model, in thread-group steps: a piece of period P costs ceil(P^2/L)
+  // tap rounds plus one for its record; an item adds zeroing + flush of its
+  // A x A accumulator.
+  auto rec_cost = [&](int r) {
+    const int L = P->cls[rank_cls[r]].L;
+    return (double)((periods[r] * periods[r] + L - 1) / L + 1);
+  };
+  auto fixed_cost = [&](int c) {
+    const ClassInfo& ci = P->cls[c];
+    return (double)(2 * ((ci.A * ci.A + ci.L - 1) / ci.L));
+  };
+  double total_cta = 0;
+  for (int64_t k = 0; k < nkeys; k++)
+    if (hist[k]) {
+      const int r = (int)(k % nper);
+      total_cta += hist[k] * rec_cost(r) / P->cls[rank_cls[r]].G;
+    }
+  const int ctas = std::max(1, sm_count() * std::max(1, P->ctas_per_sm_grid));
+  const double tau = total_cta / (4.0 * ctas);
+  std::vector<HostItem> items;
+  int64_t tiles_used = 0;
+  for (int64_t tile = 0; tile < (int64_t)P->ntx * P->nty; tile++) {
+    const int64_t k0 = tile * nper;
+    if (offs[k0 + nper] == offs[k0]) continue;
+    tiles_used++;
+    const int16_t tx = (int16_t)(tile % P->ntx), ty = (int16_t)(tile / P->ntx);
+    for (int c = 0; c < P->n_classes; c++) {
+      const double cmax = std::max(4.0 * fixed_cost(c), tau);
+      HostItem cur{};
+      bool open = false;
+      for (int r = 0; r < nper; r++) {
+        if (rank_cls[r] != c) continue;
+        int32_t pos = offs[k0 + r];
+        const int32_t end = offs[k0 + r + 1];
+        const double rcst = rec_cost(r);
+        while (pos < end) {
+          if (!open) {
+            cur.it.start = pos;
+            cur.it.count = 0;
+            cur.it.tile_x = tx;
+            cur.it.tile_y = ty;
+            cur.it.pmax = 0;
+            cur.it.cls = (int16_t)c;
+            cur.cost = fixed_cost(c);
+            open = true;
+          }
+          int64_t room = (int64_t)((cmax - cur.cost) / rcst);
+          if (room < 1) room = 1;
+          const int32_t take = (int32_t)std::min<int64_t>(room, end - pos);
+          cur.it.count += take;
+          cur.it.pmax = (int16_t)std::max<int>(cur.it.pmax, periods[r]);
+          cur.cost += take * rcst;
+          pos += take;
+          if (cur.cost >= cmax) {
+            items.push_back(cur);
+            open = false;
+          }
+        }
+      }
+      if (open) items.push_back(cur);
+    }
+  }
+  P->tiles_used = tiles_used;
+  // bundles: per class, items by decreasing cost, G at a time; then all
+  // bundles by decreasing cost (longest first).
+  std::vector<Item> it_sorted;
+  struct HB {
+    Bundle b;
+    double cost;
+  };
+  std::vector<HB> bundles;
+  for (int c = 0; c < P->n_classes; c++) {
+    std::vector<HostItem> ci;
+    for (auto& h : items)
+      if (h.it.cls == c) ci.push_back(h);
+    std::stable_sort(ci.begin(), ci.end(),
+                     [](const HostItem& a, const HostItem& b) { return a.cost > b.cost; });
+    const int G = P->cls[c].G;
+    for (size_t i = 0; i < ci.size(); i += G) {
+      HB hb;
+      hb.b.first_item = (int32_t)it_sorted.size();
+      hb.b.n_items = (int16_t)std::min<size_t>(G, ci.size() - i);
+      hb.b.cls = (int16_t)c;
+      hb.cost = ci[i].cost;
+      for (int g = 0; g < hb.b.n_items; g++) it_sorted.push_back(ci[i + g].it);
+      bundles.push_back(hb);
+    }
+  }
+  std::stable_sort(bundles.begin(), bundles.end(),
+                   [](const HB& a, const HB& b) { return a.cost > b.cost; });
+  std::vector<Bundle> bvec;
+  for (auto& hb : bundles) bvec.push_back(hb.b);
+  P->n_items = (int)it_sorted.size();
+  P->n_bundles = (int)bvec.size();
+
+  // ---- fill
+  if ((rc = dalloc(&P->d_recs, P->n_recs)) || (rc = dalloc(&P->d_items, P->n_items)) ||
+      (rc = dalloc(&P->d_bundles, P->n_bundles)))
+    return rc;
+  GB_CUDA_TRY(cudaMemcpyAsync(d_offs, offs.data(), sizeof(int32_t) * (nkeys + 1),
+                              cudaMemcpyHostToDevice, s));
+  GB_CUDA_TRY(cudaMemsetAsync(d_hist, 0, sizeof(int32_t) * nkeys, s));  // reused as cursor
+  if (P->n_items)
+    GB_CUDA_TRY(cudaMemcpyAsync(P->d_items, it_sorted.data(), sizeof(Item) * P->n_items,
+                                cudaMemcpyHostToDevice, s));
+  if (P->n_bundles)
+    GB_CUDA_TRY(cudaMemcpyAsync(P->d_bundles, bvec.data(), sizeof(Bundle) * P->n_bundles,
+                                cudaMemcpyHostToDevice, s));
+  if (n_vis > 0 && P->n_recs > 0) {
+    k_plan_fill<<<blocks_for(n_vis, 256), 256, 0, s>>>(D, P->d_planes, P->T, P->ntx, nper, d_offs,
+                                                       d_hist, P->d_recs);
+    GB_CUDA_TRY(cudaGetLastError());
+  }
+  GB_CUDA_TRY(cudaStreamSynchronize(s));
+  return GB_OK;
+}
+
+}  // namespace gb
+
+using namespace gb;
+
+extern "C" int gb_plan_create(const gb_geometry* geo, int64_t n_vis, const double* d_uvw,
+                              int64_t uvw_stride, const int32_t* d_plane, void* stream,
+                              gb_plan** out) {
+  if (!out) {
+    gb_set_error(GB_ERR_ARG, "gb_plan_create: NULL out");
+    return GB_ERR_ARG;
+  }
+  *out = nullptr;
+  if (!geo || n_vis < 0 || n_vis > (int64_t)INT32_MAX || (n_vis > 0 && !d_uvw) ||
+      uvw_stride < 3 || geo->n_planes < 1 || geo->n_planes > GB_MAX_PLANES || !geo->supports ||
+      !geo->gcf_offsets || geo->ext_x <= 0 || geo->ext_y <= 0 || geo->pitch < geo->ext_x ||
+      !(geo->scale == geo->scale)) {
+    gb_set_error(GB_ERR_ARG, "gb_plan_create: bad geometry or arguments");
+    return GB_ERR_ARG;
+  }
+  int smax = 0;
+  for (int p = 0; p < geo->n_planes; p++) {
+    const int S = geo->supports[p];
+    if (S < 1 || S > GB_MAX_SUPPORT || geo->gcf_offsets[p] < 0) {
+      gb_set_error(GB_ERR_ARG, "gb_plan_create: plane %d support %d / offset out of range", p, S);
+      return GB_ERR_ARG;
+    }
+    smax = std::max(smax, S);
+  }
+  const int T = geo->tile ? geo->tile : 32;
+  const int NT = geo->threads ? geo->threads : 256;
+  const int cap = geo->period_cap ? geo->period_cap : 32;
+  if (T < 8 || T > 128 || (NT != 128 && NT != 256 && NT != 512) || cap < 8 || cap > 64 ||
+      cap * cap > 8 * NT || geo->ext_x > 32767 * T || geo->ext_y > 32767 * T) {
+    gb_set_error(GB_ERR_ARG, "gb_plan_create: unsupported tuning tile=%d threads=%d cap=%d", T, NT,
+                 cap);
+    return GB_ERR_ARG;
+  }
+  gb_plan* P = new gb_plan();
+  GB_CUDA_TRY(cudaGetDevice(&P->device));
+  P->T = T;
+  P->NT = NT;
+  P->pcap = cap;
+  P->n_planes = geo->n_planes;
+  P->max_support = smax;
+  P->supports.assign(geo->supports, geo->supports + geo->n_planes);
+  P->gcf_offsets.assign(geo->gcf_offsets, geo->gcf_offsets + geo->n_planes);
+  const int rc = build_plan(P, geo, n_vis, d_uvw, uvw_stride, d_plane, (cudaStream_t)stream);
+  if (rc) {
+    free_plan(P);
+    return rc;
+  }
+  *out = P;
+  return GB_OK;
+}
+
+extern "C" int gb_plan_destroy(gb_plan* plan) {
+  free_plan(plan);
+  return GB_OK;
+}
+
+extern "C" int gb_plan_stats(const gb_plan* P, int64_t* st) {
+  if (!P || !st) {
+    gb_set_error(GB_ERR_ARG, "gb_plan_stats: NULL argument");
+    return GB_ERR_ARG;
+  }
+  st[0] = P->kept;
+  st[1] = P->taps;
+  st[2] = P->n_items;
+  st[3] = P->tiles_used;
+  st[4] = P->T;
+  st[5] = P->max_support;
+  st[6] = P->NT;
+  return GB_OK;
+}
+
+extern "C" int gb_plan_export_index(const gb_plan* P, int32_t* d_out5, void* stream) {
+  if (!P || !d_out5) {
+    gb_set_error(GB_ERR_ARG, "gb_plan_export_index: NULL argument");
+    return GB_ERR_ARG;
+  }
+  if (P->dev.n_vis == 0) return GB_OK;
+  k_plan_export<<<blocks_for(P->dev.n_vis, 256), 256, 0, (cudaStream_t)stream>>>(
+      P->dev, P->d_supports, d_out5);
+  GB_CUDA_TRY(cudaGetLastError());
+  return GB_OK;
+}
+
+extern "C" int gb_grid_f64(gb_plan* P, const double* d_vis, const double* d_gcf, double* d_grid,
+                           void* stream) {
+  if (!P || (P->dev.n_vis && (!d_vis || !d_gcf)) || !d_grid) {
+    gb_set_error(GB_ERR_ARG, "gb_grid_f64: NULL argument");
+    return GB_ERR_ARG;
+  }
+  if (P->dev.n_vis == 0) return GB_OK;
+  return launch_grid_plain64(P, d_vis, d_gcf, d_grid, (cudaStream_t)stream);
+}
+
+extern "C" int gb_degrid_f64(gb_plan* P, const double* d_gcf, const double* d_grid, double* d_pred,
+                             int32_t mode, void* stream) {
+  if (!P || (P->dev.n_vis && (!d_pred || !d_gcf || !d_grid)) || (mode != 0 && mode != 1)) {
+    gb_set_error(GB_ERR_ARG, "gb_degrid_f64: bad argument");
+    return GB_ERR_ARG;
+  }
+  if (P->dev.n_vis == 0) return GB_OK;
+  return launch_degrid_plain64(P, d_gcf, d_grid, d_pred, mode, (cudaStream_t)stream);
+}

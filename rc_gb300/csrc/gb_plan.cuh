@@ -1,0 +1,121 @@
+// Visibility plan: device layout of the sorted / binned work of the FP32
+// tiled kernels, and the parameters shared with the plain FP64 kernels.
+//
+// Layout in HBM (per plan):
+//   plane[n_vis]        int32  w-plane of each visibility (or -1)
+//   recs[n_recs]        Rec    16-byte records sorted by (grid tile, period)
+//   items[n_items]      Item   a contiguous record range of one tile and one
+//                              thread-group class
+//   bundles[n_bundles]  Bundle up to NT/L items run side by side in one CTA
+//   queue[2]            int32  work-queue heads (grid, degrid)
+//
+// A record is one rectangular piece (<= P x P taps) of one visibility's
+// S x S footprint: supports larger than the period cap are cut into k x k
+// pieces, k = ceil(S / cap), period P = ceil(S / k), so that every tile
+// accumulator stays within shared memory whatever the support.
+#pragma once
+
+#include <stdint.h>
+
+#include <vector>
+
+#include "gb_common.cuh"
+
+namespace gb {
+
+struct PlanDev {
+  int64_t n_vis;
+  const double* uvw;
+  int64_t uvw_stride;
+  const int32_t* plane;        // per visibility
+  const int32_t* supports;     // per plane
+  const int64_t* gcf_offsets;  // per plane
+  double scale;
+  int32_t grid_size, margin, ext_x, ext_y;
+  int64_t pitch;
+};
+
+struct __align__(16) Rec {
+  int32_t vis;     // visibility index
+  uint32_t gcf;    // complex offset of the piece's first tap in the GCF array
+  uint8_t xl, yl;  // piece corner relative to the tile origin
+  uint8_t wx, wy;  // piece extent (<= P)
+  uint8_t xm, ym;  // absolute piece corner mod P
+  uint8_t pm1;     // period P - 1
+  uint8_t sm1;     // support S - 1 (GCF row pitch); S > P marks a cut footprint
+};
+static_assert(sizeof(Rec) == 16, "Rec must be 16 bytes");
+
+struct __align__(16) Item {
+  int32_t start, count;    // record range
+  int16_t tile_x, tile_y;  // tile indices
+  int16_t pmax, cls;       // largest period in the item, thread-group class
+};
+static_assert(sizeof(Item) == 16, "Item must be 16 bytes");
+
+struct __align__(8) Bundle {
+  int32_t first_item;
+  int16_t n_items, cls;
+};
+
+// One thread-group class: L threads per group, G groups per CTA, region edge A.
+struct ClassInfo {
+  int32_t L, G, A, pmax;
+};
+
+constexpr int kMaxClasses = 4;
+
+struct PlaneInfo {
+  int32_t S, P, k, rank;
+  int64_t gcf_off;
+};
+
+}  // namespace gb
+
+struct gb_plan {
+  gb::PlanDev dev;
+  int device = 0;
+  int T = 32;       // tile edge
+  int NT = 256;     // threads per CTA of the tiled kernels
+  int pcap = 32;    // period cap
+  int n_planes = 0;
+  int max_support = 0;
+  int ntx = 0, nty = 0;
+  std::vector<int32_t> supports;
+  std::vector<int64_t> gcf_offsets;
+  std::vector<gb::PlaneInfo> planes;
+  int n_classes = 0;
+  gb::ClassInfo cls[gb::kMaxClasses] = {};
+  size_t smem_grid = 0, smem_degrid = 0;
+  int ctas_per_sm_grid = 1, ctas_per_sm_degrid = 1;
+  // device arrays owned by the plan
+  int32_t* d_plane = nullptr;
+  int32_t* d_supports = nullptr;
+  int64_t* d_offsets = nullptr;
+  gb::PlaneInfo* d_planes = nullptr;
+  gb::Rec* d_recs = nullptr;
+  gb::Item* d_items = nullptr;
+  gb::Bundle* d_bundles = nullptr;
+  int32_t* d_queue = nullptr;
+  int64_t n_recs = 0;
+  int n_items = 0, n_bundles = 0;
+  int64_t kept = 0, taps = 0, tiles_used = 0;
+  bool own_plane = true;
+};
+
+namespace gb {
+int launch_grid_plain64(const gb_plan* plan, const double* vis, const double* gcf, double* grid,
+                        cudaStream_t s);
+int launch_degrid_plain64(const gb_plan* plan, const double* gcf, const double* grid,
+                          double* pred, int mode, cudaStream_t s);
+int launch_grid_tiled(gb_plan* plan, const float* vis, const float* gcf, float* grid,
+                      cudaStream_t s);
+int launch_degrid_tiled(gb_plan* plan, const float* gcf, const float* grid, float* pred,
+                        int mode, cudaStream_t s);
+// Shared-memory bytes of the tiled kernels for a class table.
+size_t tiled_smem_grid(const ClassInfo* cls, int n_classes, int NT);
+size_t tiled_smem_degrid(const ClassInfo* cls, int n_classes, int NT);
+int tiled_max_smem();
+// Resident CTAs per SM of the tiled grid (or degrid) kernel for this plan.
+int tiled_ctas_per_sm(const gb_plan* plan, bool grid);
+}  // namespace gb

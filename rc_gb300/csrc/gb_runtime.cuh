@@ -1,0 +1,20 @@
+// Internal runtime helpers shared by the translation units of librc_gb300.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+
+namespace gb {
+
+constexpr int kStageSlots = 6;
+
+// Per-host-thread stream and grow-only device buffers used by the synchronous
+// reference-ABI entry points.
+int stage_stream(cudaStream_t* out);
+int stage_buffer(int slot, size_t bytes, void** out);
+
+int sm_count();
+
+__global__ void k_zero_f32x2(float2* __restrict__ p, int64_t n);
+
+}  // namespace gb

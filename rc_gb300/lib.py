@@ -1,0 +1,134 @@
+"""ctypes binding of librc_gb300.so (the C ABI declared in include/rc_gb300.h).
+
+The library is the only compute path: if it is missing this module raises at
+load time; there is no Python or CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "librc_gb300.so")
+
+GB_OK = 0
+ERR_SCATTER_SIZE = -444
+ERR_DEGRID_SIZE = -555
+ERR_SCATTER_GPU_SIZE = -222
+ERR_DEGRID_GPU_SIZE = -333
+ERR_ARG = -1001
+ERR_CUDA = -1002
+ERR_TIMEOUT = -1003
+ERR_NOMEM = -1004
+ERR_CAPACITY = -1005
+
+MAX_SUPPORT = 256
+MAX_PLANES = 4096
+
+
+class BufferT(C.Structure):
+    """Legacy Halide buffer_t, 72 bytes (MS6/kernel/common/halide_buf.h:17-27)."""
+
+    _fields_ = [
+        ("dev", C.c_uint64),
+        ("host", C.c_void_p),
+        ("extent", C.c_int32 * 4),
+        ("stride", C.c_int32 * 4),
+        ("min", C.c_int32 * 4),
+        ("elem_size", C.c_int32),
+        ("host_dirty", C.c_bool),
+        ("dev_dirty", C.c_bool),
+        ("_padding", C.c_uint8 * 2),
+    ]
+
+
+assert C.sizeof(BufferT) == 72
+
+
+class Geometry(C.Structure):
+    _fields_ = [
+        ("scale", C.c_double),
+        ("grid_size", C.c_int32),
+        ("margin", C.c_int32),
+        ("ext_x", C.c_int32),
+        ("ext_y", C.c_int32),
+        ("pitch", C.c_int64),
+        ("n_planes", C.c_int32),
+        ("tile", C.c_int32),
+        ("threads", C.c_int32),
+        ("period_cap", C.c_int32),
+        ("supports", C.POINTER(C.c_int32)),
+        ("gcf_offsets", C.POINTER(C.c_int64)),
+        ("w_low", C.c_double),
+        ("w_high", C.c_double),
+    ]
+
+
+# every exported symbol of include/rc_gb300.h: name -> (restype, argtypes)
+_VP = C.c_void_p
+_BP = C.POINTER(BufferT)
+SIGNATURES = {
+    "gb_last_error": (C.c_char_p, []),
+    "gb_version": (C.c_char_p, []),
+    "kern_scatter_gpu1": (C.c_int, [C.c_double, C.c_int32, C.c_int32, _BP, _BP, _BP]),
+    "kern_scatter": (C.c_int, [C.c_double, C.c_int32, C.c_int32, _BP, _BP, _BP]),
+    "nvGridder": (C.c_int, [C.c_double, C.c_int32, C.c_int32, _BP, _BP, _BP]),
+    "kern_degrid_gpu1": (C.c_int, [C.c_double, C.c_int32, C.c_int32, _BP, _BP, _BP, _BP]),
+    "kern_degrid": (C.c_int, [C.c_double, C.c_int32, C.c_int32, _BP, _BP, _BP, _BP]),
+    "kern_init": (C.c_int, [_BP]),
+    "kern_psf_vis": (C.c_int, [_BP, _BP]),
+    "gb_plan_create": (C.c_int, [C.POINTER(Geometry), C.c_int64, _VP, C.c_int64, _VP, _VP,
+                                 C.POINTER(_VP)]),
+    "gb_plan_destroy": (C.c_int, [_VP]),
+    "gb_plan_stats": (C.c_int, [_VP, C.POINTER(C.c_int64)]),
+    "gb_plan_export_index": (C.c_int, [_VP, _VP, _VP]),
+    "gb_grid_f32": (C.c_int, [_VP, _VP, _VP, _VP, _VP]),
+    "gb_degrid_f32": (C.c_int, [_VP, _VP, _VP, _VP, C.c_int32, _VP]),
+    "gb_degrid_forward": (C.c_int, [_VP, _VP, _VP, _VP, _VP]),
+    "gb_degrid_backward": (C.c_int, [_VP, _VP, _VP, _VP, _VP]),
+    "gb_grid_f64": (C.c_int, [_VP, _VP, _VP, _VP, _VP]),
+    "gb_degrid_f64": (C.c_int, [_VP, _VP, _VP, _VP, C.c_int32, _VP]),
+    "gb_gcf_generate": (C.c_int, [C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_int32),
+                                  C.POINTER(C.c_int64), C.c_int32, C.c_double, _VP, _VP, _VP,
+                                  _VP]),
+    "gb_grid_zero_f32": (C.c_int, [_VP, C.c_int64, _VP]),
+}
+
+_lib = None
+
+
+class GbError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"rc_gb300 error {code}: {msg}")
+        self.code = code
+
+
+def load(path: str = LIB_PATH):
+    """Load librc_gb300.so (building it first if the sources are newer)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path) or os.environ.get("RC_GB300_AUTOBUILD", "1") == "1":
+        try:
+            from . import build as _b
+            _b.build()
+        except Exception as e:  # no toolchain: a prebuilt library must exist
+            if not os.path.exists(path):
+                raise RuntimeError(f"librc_gb300.so is missing and could not be built: {e}")
+    L = C.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def last_error() -> str:
+    return load().gb_last_error().decode(errors="replace")
+
+
+def check(rc: int, what: str = "") -> int:
+    if rc != GB_OK:
+        raise GbError(rc, f"{what}: {last_error()}")
+    return rc

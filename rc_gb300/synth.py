@@ -1,0 +1,166 @@
+"""Seeded synthetic observations for the gridding workloads.
+
+No dataset ships with the reference (its OSKAR .vis and gcf*.dat inputs are
+not public), so every workload is generated: antenna layouts, baselines,
+earth-rotation uvw tracks over hour angle +-4 h at latitude -30 deg towards
+declination -45 deg, and visibilities of 20 point sources (l, m uniform in
++-0.05 rad, flux log-uniform 0.1-10 Jy) plus complex Gaussian noise
+sigma = 0.01.  uvw are converted from metres to wavelengths (f / c), as the
+reference's OSKAR reader does (MS6/kernel/oskar/OskarBinReader.cpp:318-385),
+and records are ordered baseline-major, time-minor.
+
+Workloads (sizes as the benchmark configurations state them):
+  c1  64 antennas uniform in a 3 km disk, 2016 bl x 256 t x 1 ch @150 MHz
+      = 516,096 vis, 2048^2 grid, one plane, 7x7 PSWF GCF padded to S=8.
+  c2  256 antennas log-radial (dense 1 km core, out to 10 km),
+      32,640 bl x 128 t = 4,177,920 vis, 4096^2 grid, 32 w-planes, S 8..64.
+  c4  c1's array, 2,064,384 vis (2016 bl x 1024 t), 2048^2 grid,
+      16 w-planes, S 8..64 (the least-squares imaging layout).
+  c5  512 stations log-radial to 40 km, 130,816 bl x 64 t x 4 ch,
+      8192^2 grid, 64 w-planes, S 8..128.
+"""
+from __future__ import annotations
+
+import dataclasses
+import math
+
+import numpy as np
+
+C_LIGHT = 299792458.0
+SEED0 = 20261203
+
+
+@dataclasses.dataclass
+class Observation:
+    name: str
+    uvw: np.ndarray  # (N, 3) float64, wavelengths
+    vis: np.ndarray  # (N,) complex128
+    grid_size: int
+    scale: float  # reference `scale`: FoV in radians (pixel = 1/scale wavelengths)
+    n_planes: int
+    supports: np.ndarray  # int32 per plane
+    w_planes: np.ndarray  # float64 GCF w per plane
+    w_low: float
+    w_high: float
+    max_support: int
+    n_bl: int
+    n_t: int
+    n_ch: int
+
+    @property
+    def n(self):
+        return self.uvw.shape[0]
+
+    def vis5(self):
+        """The reference's 5-double record (u, v, w, re, im) per visibility."""
+        out = np.empty((self.n, 5), np.float64)
+        out[:, :3] = self.uvw
+        out[:, 3] = self.vis.real
+        out[:, 4] = self.vis.imag
+        return out
+
+
+def antennas_disk(rng, n, diameter_m):
+    r = 0.5 * diameter_m * np.sqrt(rng.uniform(0, 1, n))
+    a = rng.uniform(0, 2 * np.pi, n)
+    return np.stack([r * np.cos(a), r * np.sin(a)], 1)
+
+
+def antennas_logradial(rng, n, r_core_m, r_max_m):
+    """Radii log-uniform between r_core/20 and r_max: half the stations fall
+    inside ~sqrt(r_core r_max)/..., a dense core with a sparse tail."""
+    r = np.exp(rng.uniform(np.log(r_core_m / 20.0), np.log(r_max_m), n))
+    a = rng.uniform(0, 2 * np.pi, n)
+    return np.stack([r * np.cos(a), r * np.sin(a)], 1)
+
+
+def uvw_tracks(ant_en, n_t, lat_deg=-30.0, dec_deg=-45.0, ha_hours=4.0):
+    """(n_bl, n_t, 3) metres; baselines i<j, hour angle linspace(-ha, ha, n_t)."""
+    na = ant_en.shape[0]
+    i, j = np.triu_indices(na, 1)
+    d = ant_en[j] - ant_en[i]  # east, north
+    lat = math.radians(lat_deg)
+    dec = math.radians(dec_deg)
+    X = -math.sin(lat) * d[:, 1]
+    Y = d[:, 0]
+    Z = math.cos(lat) * d[:, 1]
+    H = np.linspace(-ha_hours, ha_hours, n_t) * (np.pi / 12.0)
+    sH, cH = np.sin(H)[None, :], np.cos(H)[None, :]
+    X, Y, Z = X[:, None], Y[:, None], Z[:, None]
+    u = sH * X + cH * Y
+    v = -math.sin(dec) * cH * X + math.sin(dec) * sH * Y + math.cos(dec) * Z
+    w = math.cos(dec) * cH * X - math.cos(dec) * sH * Y + math.sin(dec) * Z
+    return np.stack([u, v, w], -1)
+
+
+def sky(rng, n_src=20, lm_max=0.05):
+    l = rng.uniform(-lm_max, lm_max, n_src)
+    m = rng.uniform(-lm_max, lm_max, n_src)
+    flux = np.exp(rng.uniform(np.log(0.1), np.log(10.0), n_src))
+    return l, m, flux
+
+
+def predict(uvw, l, m, flux, rng, noise=0.01, chunk=1 << 20):
+    n = uvw.shape[0]
+    nn = np.sqrt(1.0 - l * l - m * m) - 1.0
+    out = np.empty(n, np.complex128)
+    for a in range(0, n, chunk):
+        b = min(n, a + chunk)
+        ph = -2.0 * np.pi * (np.outer(uvw[a:b, 0], l) + np.outer(uvw[a:b, 1], m)
+                             + np.outer(uvw[a:b, 2], nn))
+        out[a:b] = (np.exp(1j * ph) * flux[None, :]).sum(1)
+    out += noise * (rng.standard_normal(n) + 1j * rng.standard_normal(n)) / np.sqrt(2.0)
+    return out
+
+
+def _finish(name, rng, uvw_m, freqs, grid_size, n_planes, s_min, s_max):
+    """metres -> wavelengths per channel, sky, scale, w-planes."""
+    from .gcf import plane_supports
+
+    n_bl, n_t, _ = uvw_m.shape
+    per_ch = [uvw_m.reshape(-1, 3) * (f / C_LIGHT) for f in freqs]
+    # channel-minor ordering within each (baseline, time): [bl][t][ch]
+    uvw = np.stack(per_ch, 1).reshape(-1, 3) if len(freqs) > 1 else per_ch[0]
+    l, m, flux = sky(rng)
+    vis = predict(uvw, l, m, flux, rng)
+    maxuv = float(np.sqrt(uvw[:, 0] ** 2 + uvw[:, 1] ** 2).max())
+    scale = 0.9 * (grid_size / 2) / maxuv
+    if n_planes > 1:
+        w = uvw[:, 2]
+        low = min(0.0, float(w.min()))
+        high0 = max(0.0, float(w.max()))
+        high = high0 + (high0 - low) * 1e-4  # MS6/programs/Kernel/Binning.hs:60
+        supports, centres = plane_supports(low, high, n_planes, s_min, s_max)
+    else:
+        low, high = -np.inf, np.inf
+        supports, centres = np.array([s_min], np.int32), np.zeros(1)
+    return Observation(name, np.ascontiguousarray(uvw), vis, grid_size, scale, n_planes,
+                       supports, centres, low, high, int(supports.max()), n_bl, n_t, len(freqs))
+
+
+def config(name: str, seed: int | None = None, n_t: int | None = None) -> Observation:
+    """Build a workload by name ('c1', 'c2', 'c4', 'c5'; 'small' for tests).
+    n_t overrides the number of time samples (for reduced test sizes)."""
+    idx = {"c1": 1, "c2": 2, "c4": 4, "c5": 5, "small": 0}[name]
+    rng = np.random.default_rng(SEED0 + idx if seed is None else seed)
+    if name == "c1":
+        ant = antennas_disk(rng, 64, 3000.0)
+        uvw_m = uvw_tracks(ant, n_t or 256)
+        return _finish(name, rng, uvw_m, [150e6], 2048, 1, 8, 8)
+    if name == "c2":
+        ant = antennas_logradial(rng, 256, 1000.0, 10000.0)
+        uvw_m = uvw_tracks(ant, n_t or 128)
+        return _finish(name, rng, uvw_m, [150e6], 4096, 32, 8, 64)
+    if name == "c4":
+        ant = antennas_disk(rng, 64, 3000.0)
+        uvw_m = uvw_tracks(ant, n_t or 1024)
+        return _finish(name, rng, uvw_m, [150e6], 2048, 16, 8, 64)
+    if name == "c5":
+        ant = antennas_logradial(rng, 512, 1000.0, 40000.0)
+        uvw_m = uvw_tracks(ant, n_t or 64)
+        freqs = [150e6 * (1 + 0.01 * k) for k in range(4)]
+        return _finish(name, rng, uvw_m, freqs, 8192, 64, 8, 128)
+    # small: quick w-projection case for tests
+    ant = antennas_logradial(rng, 24, 300.0, 3000.0)
+    uvw_m = uvw_tracks(ant, n_t or 32)
+    return _finish(name, rng, uvw_m, [150e6], 512, 8, 8, 32)

@@ -1,0 +1,71 @@
+"""The C ABI library builds, loads, and exports every entry point that
+include/rc_gb300.h declares; buffer_t has the reference's byte layout.  No
+compute calls (these run without a GPU)."""
+import ctypes as C
+import os
+import re
+import subprocess
+
+import pytest
+
+from rc_gb300 import lib
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "rc_gb300.h")
+
+
+def declared_functions():
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    names = re.findall(r"^\s*(?:const\s+)?\w+\s*\**\s*(\w+)\s*\(", src, flags=re.M)
+    return sorted(set(n for n in names if n not in ("if", "sizeof")))
+
+
+def test_header_declares_the_reference_slots():
+    names = declared_functions()
+    for ref in ["kern_scatter_gpu1", "kern_degrid_gpu1", "nvGridder", "kern_scatter",
+                "kern_degrid", "kern_init", "kern_psf_vis"]:
+        assert ref in names
+
+
+def test_library_exports_every_declared_symbol():
+    L = lib.load()
+    for name in declared_functions():
+        assert hasattr(L, name), name
+    # and the binding table covers them all
+    assert set(declared_functions()) <= set(lib.SIGNATURES)
+
+
+def test_exported_symbols_have_c_linkage():
+    out = subprocess.run(["nm", "-D", "--defined-only", lib.LIB_PATH], capture_output=True,
+                         text=True, check=True).stdout
+    exported = {line.split()[-1] for line in out.splitlines() if " T " in line}
+    for name in declared_functions():
+        assert name in exported, name
+
+
+def test_buffer_t_layout_matches_reference_offsets():
+    # offsets written by MS6/dna/flow/Flow/Halide/BufferT.hs:26-99
+    B = lib.BufferT
+    assert C.sizeof(B) == 72
+    assert B.host.offset == 8
+    assert B.extent.offset == 16
+    assert B.stride.offset == 32
+    assert B.min.offset == 48
+    assert B.elem_size.offset == 64
+    assert B.host_dirty.offset == 68
+    assert B.dev_dirty.offset == 69
+
+
+def test_version_and_error_string_without_gpu():
+    L = lib.load()
+    assert b"sm_103a" in L.gb_version()
+    assert isinstance(L.gb_last_error(), bytes)
+
+
+def test_legacy_codes_are_the_reference_values():
+    assert (lib.ERR_SCATTER_SIZE, lib.ERR_DEGRID_SIZE, lib.ERR_SCATTER_GPU_SIZE,
+            lib.ERR_DEGRID_GPU_SIZE) == (-444, -555, -222, -333)
+    hdr = open(HEADER).read()
+    for code in ["-444", "-555", "-222", "-333"]:
+        assert f"({code})" in hdr
