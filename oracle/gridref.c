@@ -301,7 +301,7 @@ void orc_wbin(int64_t n, const double *uvw, int64_t uvw_stride, double low, doub
     if (!(w >= low && w <= high)) { out[t] = -1; continue; }
     if (bins <= 1 || !(high > low)) { out[t] = 0; continue; } /* degenerate range */
     double b = floor((w - low) / (high - low) * (double)bins);
-    int32_t bi = b < 0 ? 0 : (b > bins - 1 ? bins - 1 : (int32_t)b);
+    int32_t bi = !(b >= 0) ? 0 : (b > bins - 1 ? bins - 1 : (int32_t)b); /* NaN -> 0 */
     out[t] = bi;
   }
 }

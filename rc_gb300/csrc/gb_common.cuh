@@ -70,7 +70,8 @@ __host__ __device__ __forceinline__ int32_t w_plane(double w, double low, double
   if (!(w >= low && w <= high)) return -1;
   if (bins <= 1 || !(high > low)) return 0;
   const double b = floor((w - low) / (high - low) * (double)bins);
-  return b < 0.0 ? 0 : (b > (double)(bins - 1) ? bins - 1 : (int32_t)b);
+  if (!(b >= 0.0)) return 0;  // also an infinite range (NaN)
+  return b > (double)(bins - 1) ? bins - 1 : (int32_t)b;
 }
 
 }  // namespace gb
