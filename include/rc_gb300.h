@@ -194,6 +194,41 @@ int gb_gcf_generate(int32_t n_planes, const double *w_planes, const int32_t *sup
                     const int64_t *gcf_offsets, int32_t max_support, double t2,
                     const double *d_taper, double *d_gcf64, float *d_gcf32, void *stream);
 
+/* Allocation-free gridding.  No counterpart in the reference.
+ *
+ * For callers that cannot call cudaMalloc: code running inside a host
+ * framework that owns all device memory (a pipeline runtime with a fixed
+ * budget or pool, a plugin of another GPU application), or real-time paths
+ * where an allocation's latency or failure is not acceptable.  It does what
+ * gb_plan_create + gb_grid_f32 + gb_plan_destroy do together (grid += G vis,
+ * same FP32 tiled kernel, same tolerance) for one batch of visibilities, and
+ * calls no cudaMalloc, cudaFree or allocating library routine: its working
+ * memory is one static device array of GB_NOALLOC_SCRATCH_BYTES (7 MiB),
+ * which every GPU that loads this library holds until the process exits.
+ * The caller passes inputs and the output grid (device pointers, as for
+ * gb_plan_create / gb_grid_f32).
+ *
+ * Limits: at most GB_NOALLOC_MAX_VIS visibilities, GB_NOALLOC_MAX_PLANES
+ * planes, n_vis * k^2 <= GB_NOALLOC_MAX_PIECES footprint pieces (k = pieces
+ * per axis of the largest support, ceil(S / period_cap)), and at most
+ * GB_NOALLOC_MAX_BINS (grid tile, thread-group class) bins; larger requests
+ * return GB_ERR_CAPACITY before any GPU work.
+ *
+ * The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * Every call on a device shares the array and leaves its contents behind; each
+ * call clears what must start at zero.  Calls whose GPU work overlaps (other
+ * streams, other host threads) race on the array: serialise them.  The call
+ * synchronises `stream` once (to size the kernel launch). */
+#define GB_NOALLOC_MAX_VIS (1 << 17)
+#define GB_NOALLOC_MAX_PIECES (1 << 18)
+#define GB_NOALLOC_MAX_BINS (1 << 16)
+#define GB_NOALLOC_MAX_PLANES 256
+#define GB_NOALLOC_SCRATCH_BYTES (7 << 20)
+int gb_grid_f32_noalloc(const gb_geometry *geo, int64_t n_vis, const double *d_uvw,
+                        int64_t uvw_stride, const int32_t *d_plane, const float *d_vis,
+                        const float *d_gcf, float *d_grid, void *stream);
+
 /* Zero `n_complex` complex64 grid elements (device). */
 int gb_grid_zero_f32(float *d_grid, int64_t n_complex, void *stream);
 

@@ -116,6 +116,10 @@ int launch_degrid_tiled(gb_plan* plan, const float* gcf, const float* grid, floa
 size_t tiled_smem_grid(const ClassInfo* cls, int n_classes, int NT);
 size_t tiled_smem_degrid(const ClassInfo* cls, int n_classes, int NT);
 int tiled_max_smem();
+int launch_grid_tiled_tables(const Bundle* bundles, int n_bundles, const Item* items,
+                             const Rec* recs, int32_t* queue, const ClassInfo* cls, int n_classes,
+                             int NT, int T, int ext_x, int ext_y, int64_t pitch, size_t smem,
+                             const float* vis, const float* gcf, float* grid, cudaStream_t s);
 // Resident CTAs per SM of the tiled grid (or degrid) kernel for this plan.
 int tiled_ctas_per_sm(const gb_plan* plan, bool grid);
 }  // namespace gb

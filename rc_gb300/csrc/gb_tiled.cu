@@ -432,6 +432,41 @@ int launch_degrid_tiled(gb_plan* P, const float* gcf, const float* grid, float* 
   return GB_OK;
 }
 
+// Launch of the tiled gridding kernel on caller-supplied work tables (used by
+// the allocation-free entry point, whose tables live in a static device
+// array rather than in a plan).
+int launch_grid_tiled_tables(const Bundle* bundles, int n_bundles, const Item* items,
+                             const Rec* recs, int32_t* queue, const ClassInfo* cls, int n_classes,
+                             int NT, int T, int ext_x, int ext_y, int64_t pitch, size_t smem,
+                             const float* vis, const float* gcf, float* grid, cudaStream_t s) {
+  if (n_bundles <= 0) return GB_OK;
+  int R = 1;
+  for (int c = 0; c < n_classes; c++)
+    R = std::max(R, (cls[c].pmax * cls[c].pmax + cls[c].L - 1) / cls[c].L);
+  R = R <= 1 ? 1 : R <= 2 ? 2 : R <= 4 ? 4 : 8;
+  GridFn fn = grid_fn(NT, R);
+  int rc = set_smem_attr((const void*)fn);
+  if (rc) return rc;
+  int per_sm = 0;
+  GB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, NT, smem));
+  const int blocks = std::min(n_bundles, sm_count() * std::max(1, per_sm));
+  TiledArgs a;
+  a.bundles = bundles;
+  a.items = items;
+  a.recs = recs;
+  a.queue = queue;
+  for (int c = 0; c < kMaxClasses; c++) a.cls[c] = c < n_classes ? cls[c] : ClassInfo{64, 1, 1, 1};
+  a.n_bundles = n_bundles;
+  a.T = T;
+  a.ext_x = ext_x;
+  a.ext_y = ext_y;
+  a.pitch = pitch;
+  GB_CUDA_TRY(cudaMemsetAsync(queue, 0, sizeof(int32_t), s));
+  fn<<<blocks, NT, smem, s>>>(a, (const float2*)vis, (const float2*)gcf, (float2*)grid);
+  GB_CUDA_TRY(cudaGetLastError());
+  return GB_OK;
+}
+
 }  // namespace gb
 
 using namespace gb;

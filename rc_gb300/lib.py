@@ -23,6 +23,10 @@ ERR_NOMEM = -1004
 ERR_CAPACITY = -1005
 
 MAX_SUPPORT = 256
+NOALLOC_MAX_VIS = 1 << 17
+NOALLOC_MAX_PIECES = 1 << 18
+NOALLOC_MAX_BINS = 1 << 16
+NOALLOC_MAX_PLANES = 256
 MAX_PLANES = 4096
 
 
@@ -92,6 +96,8 @@ SIGNATURES = {
                                   C.POINTER(C.c_int64), C.c_int32, C.c_double, _VP, _VP, _VP,
                                   _VP]),
     "gb_grid_zero_f32": (C.c_int, [_VP, C.c_int64, _VP]),
+    "gb_grid_f32_noalloc": (C.c_int, [C.POINTER(Geometry), C.c_int64, _VP, C.c_int64, _VP, _VP,
+                                      _VP, _VP, _VP]),
 }
 
 _lib = None
