@@ -225,19 +225,46 @@ def our_arm(args):
     gcf_ms = 1e3 * (time.perf_counter() - t0)
 
     d_uvw = torch.tensor(ob.uvw, device=dev)
+    vis32 = torch.tensor(ob.vis, dtype=torch.complex64, device=dev)
+    vis64 = torch.tensor(ob.vis, dtype=torch.complex128, device=dev)
+    grid = torch.zeros((G, G), dtype=torch.complex64, device=dev)
+
+    def make_plan(**p):
+        return Plan(d_uvw, scale=ob.scale, grid_size=G, grid_shape=(G, G), supports=ob.supports,
+                    w_range=(ob.w_low, ob.w_high), **p)
+
+    # tunables: explicit flags, else the autotuner (cached per workload key)
+    from rc_gb300 import autotune as AT
+
+    explicit = {k: v for k, v in (("tile", args.tile), ("threads", args.threads),
+                                  ("period_cap", args.cap)) if v}
+    tune_info = {"source": "flags" if explicit else "autotune"}
+    if explicit or args.no_tune:
+        params = dict(AT.DEFAULT, **explicit)
+        tune_info["source"] = "flags" if explicit else "defaults"
+    else:
+        probe = make_plan(**AT.DEFAULT)
+        planes = probe.export_index()
+        kept_mask = planes[:, 4] == 1
+        counts = torch.bincount(planes[kept_mask, 3].long(), minlength=len(ob.supports)).cpu()
+        key = AT.plan_signature(probe, counts.numpy())
+        probe.close()
+        cached = AT._load().get(key)
+        if cached:
+            params, tune_info["cached"] = dict(cached["params"]), True
+        else:
+            t0 = time.perf_counter()
+            params, best_ms, table = AT.tune(make_plan, vis32, g32, grid, key=key)
+            tune_info.update(cached=False, candidates=len(table), seconds=round(
+                time.perf_counter() - t0, 2), best_ms=round(best_ms, 3))
+        tune_info["key"] = key
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    plan = Plan(d_uvw, scale=ob.scale, grid_size=G, grid_shape=(G, G), supports=ob.supports,
-                w_range=(ob.w_low, ob.w_high), tile=args.tile, threads=args.threads,
-                period_cap=args.cap)
+    plan = make_plan(**params)
     torch.cuda.synchronize()
     plan_ms = 1e3 * (time.perf_counter() - t0)
     st = plan.stats()
     kept, taps = st["kept"], st["taps"]
-
-    vis32 = torch.tensor(ob.vis, dtype=torch.complex64, device=dev)
-    vis64 = torch.tensor(ob.vis, dtype=torch.complex128, device=dev)
-    grid = torch.zeros((G, G), dtype=torch.complex64, device=dev)
     pred = torch.empty(ob.n, dtype=torch.complex64, device=dev)
     flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=dev)
 
@@ -330,7 +357,7 @@ def our_arm(args):
 
     # plain FP64 GPU path, same step
     k64 = []
-    for i in range(2 + max(2, args.steps // 4)):
+    for i in range(0 if args.quick else 2 + max(2, args.steps // 4)):
         flush.fill_(float(i))
         grid64.zero_()
         ev[0].record(s)
@@ -340,7 +367,7 @@ def our_arm(args):
         ev[1].synchronize()
         if i >= 2:
             k64.append(ev[0].elapsed_time(ev[1]))
-    fp64_mvis = ob.n / (np.mean(k64) * 1e-3) / 1e6
+    fp64_mvis = ob.n / (np.mean(k64) * 1e-3) / 1e6 if k64 else float("nan")
 
     # roofline of the dominant kernel (algorithmic bytes, unfused per-tap model)
     peak, peak_kind = measured_peaks()
@@ -369,7 +396,7 @@ def our_arm(args):
     d_vis_e = torch.empty_like(vis32)
     d_model_e = torch.empty_like(model32)
     e2e = []
-    for i in range(args.warmup + args.steps):
+    for i in range(0 if args.quick else args.warmup + args.steps):
         flush.fill_(float(i))
         ev[0].record(s)
         d_vis_e.copy_(h_vis, non_blocking=True)
@@ -383,13 +410,13 @@ def our_arm(args):
         ev[1].synchronize()
         if i >= args.warmup:
             e2e.append(ev[0].elapsed_time(ev[1]))
-    e2e_mvis = world * ob.n / (float(np.mean(e2e)) * 1e-3) / 1e6
+    e2e_mvis = world * ob.n / (float(np.mean(e2e)) * 1e-3) / 1e6 if e2e else float("nan")
     h2d = h_vis.numel() * 8 + h_model.numel() * 8
     d2h = h_grid.numel() * 8 + h_pred.numel() * 8
 
     # CPU baseline (rank 0, N = 1 only): the oracle port on the host cores
     cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu:
+    if rank == 0 and world == 1 and not args.no_cpu and not args.quick:
         offs_np, _ = Gm.layout(ob.supports)
         n, dt, used, _, _ = cpu_leg(ob, ob.supports, g64.cpu().numpy(), offs_np, args.cpu_sample,
                                     os.cpu_count() or 1)
@@ -407,6 +434,7 @@ def our_arm(args):
                        "taps": taps, "grid": f"{G}x{G} complex64",
                        "l2": "flushed (256 MiB write) before every step",
                        "tile": st["tile"], "threads": st["threads"], "graph": use_graph,
+                       "tuning": dict(params, **tune_info),
                        "parallelism": f"replicas x{world}"},
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1),
                          "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
@@ -417,11 +445,12 @@ def our_arm(args):
                            "degrid_frac_of_roofline": round(bytes_deg / (td * 1e-3) / 1e9 / peak, 4),
                            "plan_ms": round(plan_ms, 2), "gcf_generate_ms": round(gcf_ms, 2)},
             "fp64_plain": {"value": round(fp64_mvis, 3), "unit": "Mvis/s",
-                           "ms_per_step": round(float(np.mean(k64)), 3),
+                           "ms_per_step": round(float(np.mean(k64)), 3) if k64 else None,
                            "speedup_f32_over_f64": round(value / world / fp64_mvis, 2)},
             "rel_l2_vs_fp64": {"grid": err_grid, "degrid": err_deg, "bar": 1e-5},
             "e2e": {"value": round(e2e_mvis, 3), "unit": "Mvis/s", "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h, "ms_per_step": round(float(np.mean(e2e)), 3)},
+                    "d2h_bytes_per_step": d2h,
+                    "ms_per_step": round(float(np.mean(e2e)), 3) if e2e else None},
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
             "gpu_launches": 2 * args.steps,
@@ -446,7 +475,10 @@ def main(argv=None):
     ap.add_argument("--threads", type=int, default=0)
     ap.add_argument("--cap", type=int, default=0)
     ap.add_argument("--no-graph", action="store_true")
+    ap.add_argument("--no-tune", action="store_true", help="built-in defaults, no autotuning")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--quick", action="store_true",
+                    help="FP32 step, kernel times and error only (tuning sweeps)")
     ap.add_argument("--cpu-sample", type=int, default=1 << 20)
     args = ap.parse_args(argv)
     if args.warmup < 3 and args.impl == "ours":

@@ -319,7 +319,7 @@ extern "C" int gb_grid_f32_noalloc(const gb_geometry* geo, int64_t n_vis, const 
   }
   for (int c = 0; c < nwidth; c++) {
     cls[c].A = T + cls[c].pmax - 1;
-    const size_t per_group = (size_t)cls[c].A * cls[c].A * 16 + (size_t)cls[c].L * 24;
+    const size_t per_group = grid_group_bytes(cls[c].A, cls[c].L);
     int G = NT / cls[c].L;
     while (G > 0 && (size_t)G * per_group > (size_t)smem_cap) G--;
     if (G == 0) {

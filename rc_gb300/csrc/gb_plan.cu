@@ -225,7 +225,7 @@ static int build_plan(gb_plan* P, const gb_geometry* geo, int64_t n_vis, const d
     for (int r = 0; r < nper; r++)
       if (rank_cls[r] == c) ci.pmax = std::max(ci.pmax, periods[r]);
     ci.A = P->T + ci.pmax - 1;
-    const size_t per_group = (size_t)ci.A * ci.A * 16 + (size_t)ci.L * 24;
+    const size_t per_group = grid_group_bytes(ci.A, ci.L);
     int G = P->NT / ci.L;
     while (G > 0 && (size_t)G * per_group > (size_t)smem_cap) G--;
     if (G == 0) {
@@ -338,7 +338,7 @@ static int build_plan(gb_plan* P, const gb_geometry* geo, int64_t n_vis, const d
       total_cta += hist[k] * rec_cost(r) / P->cls[rank_cls[r]].G;
     }
   const int ctas = std::max(1, sm_count() * std::max(1, P->ctas_per_sm_grid));
-  const double tau = total_cta / (4.0 * ctas);
+  const double tau = total_cta / ((double)P->bpc * ctas);
   std::vector<HostItem> items;
   int64_t tiles_used = 0;
   for (int64_t tile = 0; tile < (int64_t)P->ntx * P->nty; tile++) {
@@ -468,8 +468,10 @@ extern "C" int gb_plan_create(const gb_geometry* geo, int64_t n_vis, const doubl
   const int T = geo->tile ? geo->tile : 32;
   const int NT = geo->threads ? geo->threads : 256;
   const int cap = geo->period_cap ? geo->period_cap : 32;
+  const int bpc = geo->bundles_per_cta ? geo->bundles_per_cta : 4;
   if (T < 8 || T > 128 || (NT != 128 && NT != 256 && NT != 512) || cap < 8 || cap > 64 ||
-      cap * cap > 8 * NT || geo->ext_x > 32767 * T || geo->ext_y > 32767 * T) {
+      cap * cap > 8 * NT || bpc < 1 || bpc > 64 || geo->ext_x > 32767 * T ||
+      geo->ext_y > 32767 * T) {
     gb_set_error(GB_ERR_ARG, "gb_plan_create: unsupported tuning tile=%d threads=%d cap=%d", T, NT,
                  cap);
     return GB_ERR_ARG;
@@ -479,6 +481,7 @@ extern "C" int gb_plan_create(const gb_geometry* geo, int64_t n_vis, const doubl
   P->T = T;
   P->NT = NT;
   P->pcap = cap;
+  P->bpc = bpc;
   P->n_planes = geo->n_planes;
   P->max_support = smax;
   P->supports.assign(geo->supports, geo->supports + geo->n_planes);

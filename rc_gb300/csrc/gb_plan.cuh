@@ -63,6 +63,19 @@ struct ClassInfo {
   int32_t L, G, A, pmax;
 };
 
+// Shared memory of one thread group: the A x A accumulator (float4: sum and
+// Kahan compensation) or grid stage (float2), plus one batch of L decoded
+// records (32 B each; gridding also stages the L visibility values).
+__host__ __device__ inline size_t grid_group_bytes(int A, int L) { return 16 * (size_t)A * A + 40 * (size_t)L; }
+// The float2 grid stage is padded to 16 bytes so that the 16-byte records
+// behind it (and the next group's region) stay 16-byte aligned.
+__host__ __device__ inline size_t degrid_stage_bytes(int A) {
+  return (8 * (size_t)A * A + 15) & ~(size_t)15;
+}
+__host__ __device__ inline size_t degrid_group_bytes(int A, int L) {
+  return degrid_stage_bytes(A) + 32 * (size_t)L;
+}
+
 constexpr int kMaxClasses = 4;
 
 struct PlaneInfo {
@@ -78,6 +91,7 @@ struct gb_plan {
   int T = 32;       // tile edge
   int NT = 256;     // threads per CTA of the tiled kernels
   int pcap = 32;    // period cap
+  int bpc = 4;      // target bundles per resident CTA (work granularity)
   int n_planes = 0;
   int max_support = 0;
   int ntx = 0, nty = 0;

@@ -14,16 +14,16 @@
 // (a, b) = (r mod P, r div P) of pixel coordinates mod P: piece tap (i, j)
 // lands on pixel (x0 + i, y0 + j) with i = (a - x0) mod P, so no two threads
 // ever touch the same pixel and the accumulation is a plain read-modify-write
-// with an error-free transformation (TwoSum) carrying the rounding error of
-// every addition in a second accumulator.  At the end the group adds sum +
+// with Kahan compensation carrying the rounding error of every addition in
+// a second accumulator.  At the end the group adds sum +
 // compensation into the global grid with float2 atomics, skipping pixels no
 // piece touched; atomics are needed only because neighbouring tiles'
 // overhangs and other items of the same tile overlap.
 //
 // Degridding (D = G^H): each group stages its A x A grid region in shared
 // memory with coalesced loads, then each warp takes pieces, gathers the taps
-// from shared memory, multiplies by conj(GCF), sums with per-lane TwoSum and
-// a warp-shuffle reduction.  A visibility whose footprint was cut into
+// from shared memory, multiplies by conj(GCF), sums with per-lane Kahan
+// compensation and a warp-shuffle reduction.  A visibility whose footprint was cut into
 // several pieces accumulates them with float2 atomics; otherwise a plain store.
 #include <algorithm>
 #include <mutex>
@@ -52,13 +52,13 @@ __device__ __forceinline__ void group_sync(int id, int n, bool whole_cta) {
     asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory");
 }
 
-// s + x with the rounding error accumulated into c (Knuth's TwoSum).
-__device__ __forceinline__ void two_sum(float& s, float& c, float x) {
-  const float t = __fadd_rn(s, x);
-  const float bp = __fsub_rn(t, s);
-  const float e = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bp)), __fsub_rn(x, bp));
+// Kahan step: s + x with the running compensation c (the negated lost low
+// part of earlier additions); the compensated total is s - c.
+__device__ __forceinline__ void kahan(float& s, float& c, float x) {
+  const float y = __fsub_rn(x, c);
+  const float t = __fadd_rn(s, y);
+  c = __fsub_rn(__fsub_rn(t, s), y);
   s = t;
-  c = __fadd_rn(c, e);
 }
 
 constexpr int kInvalidResidue = 1 << 14;
@@ -70,136 +70,154 @@ __device__ __forceinline__ ClassInfo class_of(const TiledArgs& a, int c) {
   return c == 0 ? a.cls[0] : c == 1 ? a.cls[1] : c == 2 ? a.cls[2] : a.cls[3];
 }
 
+// A record decoded once per batch into shared memory (32 bytes), so that the
+// threads of a group read plain ints instead of unpacking bytes per tap.
+struct __align__(16) GridRec {
+  int32_t gcf;    // GCF element offset of the piece's first tap
+  int32_t q0;     // accumulator index of the piece corner: yl * A + xl
+  int32_t xm, ym; // piece corner mod P
+  int32_t wx, wy; // piece extent
+  int32_t pitch;  // GCF row pitch (the plane's support S)
+  int32_t P;      // period of the run
+};
+
+struct __align__(16) DegridRec {
+  int32_t gcf, q0, wx, wy, pitch, vis, cut, pad;
+};
+
+// Residue slots a thread needs for period P in a group of L threads.
+__device__ __forceinline__ int slots_for(int P, int L) { return (P * P + L - 1) / L; }
+
+// One run [k, e) of equal period P of the staged batch: thread lt owns the
+// residues rr = lt + m L < P^2, (a, b) = (rr mod P, rr div P); U pieces at a
+// time, all GCF loads first, then the read-modify-writes in piece order.
 template <int R, int U>
+__device__ __forceinline__ void grid_run(int k, int e, int lt, int L, int A,
+                                         const GridRec* __restrict__ srec,
+                                         const float2* __restrict__ svis,
+                                         float4* __restrict__ acc,
+                                         const float2* __restrict__ gcf) {
+  const int P = srec[k].P;
+  int ra[R], rb[R];
+#pragma unroll
+  for (int m = 0; m < R; m++) {
+    const int rr = lt + m * L;
+    if (rr < P * P) {
+      rb[m] = rr / P;
+      ra[m] = rr - rb[m] * P;
+    } else {
+      ra[m] = kInvalidResidue;
+      rb[m] = kInvalidResidue;
+    }
+  }
+  for (; k < e; k += U) {
+    float2 c[U][R];
+    int qi[U][R];
+    float2 v[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const bool live = k + u < e;
+      const GridRec r = srec[live ? k + u : k];
+      v[u] = svis[live ? k + u : k];
+#pragma unroll
+      for (int m = 0; m < R; m++) {
+        int i = ra[m] - r.xm;
+        i += i < 0 ? P : 0;
+        int j = rb[m] - r.ym;
+        j += j < 0 ? P : 0;
+        if (live && i < r.wx && j < r.wy) {
+          c[u][m] = __ldg(gcf + r.gcf + j * r.pitch + i);
+          qi[u][m] = r.q0 + j * A + i;
+        } else {
+          c[u][m] = make_float2(0.f, 0.f);
+          qi[u][m] = -1;
+        }
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+#pragma unroll
+      for (int m = 0; m < R; m++) {
+        const int q = qi[u][m];
+        if (q >= 0) {
+          const float tr = v[u].x * c[u][m].x - v[u].y * c[u][m].y;
+          const float ti = v[u].x * c[u][m].y + v[u].y * c[u][m].x;
+          float4 s = acc[q];
+          kahan(s.x, s.z, tr);
+          kahan(s.y, s.w, ti);
+          acc[q] = s;
+        }
+      }
+    }
+  }
+}
+
+// Gridding of one item by one thread group.  acc holds A*A float4 =
+// (sum.re, sum.im, comp.re, comp.im) per pixel.
 __device__ __forceinline__ void grid_item(const TiledArgs& a, const Item& it, int lt, int L,
-                                          int bar, bool whole, int A, float2* __restrict__ sum,
-                                          float2* __restrict__ cmp, Rec* __restrict__ srec,
-                                          float2* __restrict__ svis,
+                                          int bar, bool whole, int A, float4* __restrict__ acc,
+                                          GridRec* __restrict__ srec, float2* __restrict__ svis,
                                           const float2* __restrict__ vis,
                                           const float2* __restrict__ gcf,
                                           float2* __restrict__ grid) {
   const int AA = A * A;
-  for (int q = lt; q < AA; q += L) {
-    sum[q] = make_float2(0.f, 0.f);
-    cmp[q] = make_float2(0.f, 0.f);
-  }
+  for (int q = lt; q < AA; q += L) acc[q] = make_float4(0.f, 0.f, 0.f, 0.f);
   int curP = -1;
-  int ra[R], rb[R];
   const int end = it.start + it.count;
   for (int base = it.start; base < end; base += L) {
     const int nb = min(L, end - base);
     group_sync(bar, L, whole);  // zeroing done / previous batch consumed
     if (lt < nb) {
       const Rec r = a.recs[base + lt];
-      srec[lt] = r;
+      GridRec d;
+      d.gcf = (int32_t)r.gcf;
+      d.q0 = r.yl * A + r.xl;
+      d.xm = r.xm;
+      d.ym = r.ym;
+      d.wx = r.wx;
+      d.wy = r.wy;
+      d.pitch = r.sm1 + 1;
+      d.P = r.pm1 + 1;
+      srec[lt] = d;
       svis[lt] = __ldg(vis + r.vis);
     }
     group_sync(bar, L, whole);
     int k = 0;
     while (k < nb) {
-      const int pm1 = srec[k].pm1;
-      const int P = pm1 + 1;
+      const int P = srec[k].P;
       if (P != curP) {
         // the residue map changes: finish every read-modify-write of the old one
         group_sync(bar, L, whole);
         curP = P;
-#pragma unroll
-        for (int m = 0; m < R; m++) {
-          const int rr = lt + m * L;
-          if (rr < P * P) {
-            rb[m] = rr / P;
-            ra[m] = rr - rb[m] * P;
-          } else {
-            ra[m] = kInvalidResidue;
-            rb[m] = kInvalidResidue;
-          }
-        }
       }
       int e = k + 1;
-      while (e < nb && srec[e].pm1 == pm1) e++;
-      // U pieces at a time: all GCF loads first, then the ordered RMWs
-      for (; k + U <= e; k += U) {
-        float2 c[U][R];
-        int qi[U][R];
-        float2 v[U];
-#pragma unroll
-        for (int u = 0; u < U; u++) {
-          const Rec r = srec[k + u];
-          v[u] = svis[k + u];
-          const float2* gp = gcf + r.gcf;
-          const int pitch = r.sm1 + 1;
-#pragma unroll
-          for (int m = 0; m < R; m++) {
-            int i = ra[m] - r.xm;
-            i += i < 0 ? P : 0;
-            int j = rb[m] - r.ym;
-            j += j < 0 ? P : 0;
-            if (i < r.wx && j < r.wy) {
-              c[u][m] = __ldg(gp + j * pitch + i);
-              qi[u][m] = (r.yl + j) * A + r.xl + i;
-            } else {
-              c[u][m] = make_float2(0.f, 0.f);
-              qi[u][m] = -1;
-            }
-          }
-        }
-#pragma unroll
-        for (int u = 0; u < U; u++) {
-#pragma unroll
-          for (int m = 0; m < R; m++) {
-            const int q = qi[u][m];
-            if (q >= 0) {
-              const float tr = v[u].x * c[u][m].x - v[u].y * c[u][m].y;
-              const float ti = v[u].x * c[u][m].y + v[u].y * c[u][m].x;
-              float2 s = sum[q], cc = cmp[q];
-              two_sum(s.x, cc.x, tr);
-              two_sum(s.y, cc.y, ti);
-              sum[q] = s;
-              cmp[q] = cc;
-            }
-          }
-        }
+      while (e < nb && srec[e].P == P) e++;
+      switch (slots_for(P, L)) {
+        case 1: grid_run<1, 8>(k, e, lt, L, A, srec, svis, acc, gcf); break;
+        case 2: grid_run<2, 4>(k, e, lt, L, A, srec, svis, acc, gcf); break;
+        case 3: grid_run<3, 3>(k, e, lt, L, A, srec, svis, acc, gcf); break;
+        case 4: grid_run<4, 2>(k, e, lt, L, A, srec, svis, acc, gcf); break;
+        case 5:
+        case 6: grid_run<6, 1>(k, e, lt, L, A, srec, svis, acc, gcf); break;
+        default: grid_run<8, 1>(k, e, lt, L, A, srec, svis, acc, gcf); break;
       }
-      for (; k < e; k++) {
-        const Rec r = srec[k];
-        const float2 vv = svis[k];
-        const float2* gp = gcf + r.gcf;
-        const int pitch = r.sm1 + 1;
-#pragma unroll
-        for (int m = 0; m < R; m++) {
-          int i = ra[m] - r.xm;
-          i += i < 0 ? P : 0;
-          int j = rb[m] - r.ym;
-          j += j < 0 ? P : 0;
-          if (i < r.wx && j < r.wy) {
-            const float2 c = __ldg(gp + j * pitch + i);
-            const int q = (r.yl + j) * A + r.xl + i;
-            const float tr = vv.x * c.x - vv.y * c.y;
-            const float ti = vv.x * c.y + vv.y * c.x;
-            float2 s = sum[q], cc = cmp[q];
-            two_sum(s.x, cc.x, tr);
-            two_sum(s.y, cc.y, ti);
-            sum[q] = s;
-            cmp[q] = cc;
-          }
-        }
-      }
+      k = e;
     }
   }
   group_sync(bar, L, whole);
   const int x0 = it.tile_x * a.T, y0 = it.tile_y * a.T;
   for (int q = lt; q < AA; q += L) {
-    const float2 s = sum[q], c = cmp[q];
-    if (s.x != 0.f || s.y != 0.f || c.x != 0.f || c.y != 0.f) {
+    const float4 s = acc[q];
+    if (s.x != 0.f || s.y != 0.f || s.z != 0.f || s.w != 0.f) {
       const int py = q / A, px = q - py * A;
       const int gx = x0 + px, gy = y0 + py;
       if (gx < a.ext_x && gy < a.ext_y)
-        atomicAdd(grid + (int64_t)gy * a.pitch + gx, make_float2(s.x + c.x, s.y + c.y));
+        atomicAdd(grid + (int64_t)gy * a.pitch + gx, make_float2(s.x - s.z, s.y - s.w));
     }
   }
 }
 
-template <int NT, int R, int U>
+template <int NT>
 __global__ void __launch_bounds__(NT) k_grid_tiled(TiledArgs a, const float2* __restrict__ vis,
                                                    const float2* __restrict__ gcf,
                                                    float2* __restrict__ grid) {
@@ -217,21 +235,25 @@ __global__ void __launch_bounds__(NT) k_grid_tiled(TiledArgs a, const float2* __
     if (g < bd.n_items) {
       const int lt = tid - g * ci.L;
       const int AA = ci.A * ci.A;
-      unsigned char* base = smem + (size_t)g * (16 * (size_t)AA + 24 * (size_t)ci.L);
-      float2* sum = (float2*)base;
-      float2* cmp = sum + AA;
-      Rec* srec = (Rec*)(base + 16 * (size_t)AA);
-      float2* svis = (float2*)(base + 16 * (size_t)AA + 16 * (size_t)ci.L);
-      grid_item<R, U>(a, a.items[bd.first_item + g], lt, ci.L, 1 + g, ci.L == NT, ci.A, sum, cmp,
-                      srec, svis, vis, gcf, grid);
+      unsigned char* base = smem + (size_t)g * grid_group_bytes(ci.A, ci.L);
+      float4* acc = (float4*)base;
+      GridRec* srec = (GridRec*)(base + 16 * (size_t)AA);
+      float2* svis = (float2*)(base + 16 * (size_t)AA + 32 * (size_t)ci.L);
+      grid_item(a, a.items[bd.first_item + g], lt, ci.L, 1 + g, ci.L == NT, ci.A, acc, srec,
+                svis, vis, gcf, grid);
     }
     __syncthreads();
   }
 }
 
-template <int MODE>
+// Degridding of one item: stage the A x A grid region, then batches of L
+// decoded records; sub-warps of SW lanes take one piece each (32/SW pieces
+// per warp at a time), lanes stride the piece's taps by SW, Kahan per lane,
+// shuffle reduction within the sub-warp.
+template <int MODE, int SW>
 __device__ __forceinline__ void degrid_item(const TiledArgs& a, const Item& it, int lt, int L,
                                             int bar, bool whole, int A, float2* __restrict__ sg,
+                                            DegridRec* __restrict__ srec,
                                             const float2* __restrict__ gcf,
                                             const float2* __restrict__ grid,
                                             float2* __restrict__ pred) {
@@ -243,51 +265,74 @@ __device__ __forceinline__ void degrid_item(const TiledArgs& a, const Item& it, 
     sg[q] = (gx < a.ext_x && gy < a.ext_y) ? grid[(int64_t)gy * a.pitch + gx]
                                            : make_float2(0.f, 0.f);
   }
-  group_sync(bar, L, whole);
+  constexpr int SUBS = 32 / SW;
   const int nw = L >> 5, w = lt >> 5, lane = lt & 31;
+  const int sub = lane / SW, sl = lane - sub * SW;
   const int end = it.start + it.count;
-  for (int k = it.start + w; k < end; k += nw) {
-    const Rec r = a.recs[k];
-    const int wx = r.wx, wy = r.wy, pitch = r.sm1 + 1;
-    const float2* gp = gcf + r.gcf;
-    const float2* sp = sg + r.yl * A + r.xl;
-    float ar = 0.f, ai = 0.f, cr = 0.f, ci = 0.f;
-    int j = lane / wx;
-    int i = lane - j * wx;
-    const int dj = 32 / wx, di = 32 - dj * wx;
+  for (int base = it.start; base < end; base += L) {
+    const int nb = min(L, end - base);
+    group_sync(bar, L, whole);  // staging done / previous batch consumed
+    if (lt < nb) {
+      const Rec r = a.recs[base + lt];
+      DegridRec d;
+      d.gcf = (int32_t)r.gcf;
+      d.q0 = r.yl * A + r.xl;
+      d.wx = r.wx;
+      d.wy = r.wy;
+      d.pitch = r.sm1 + 1;
+      d.vis = r.vis;
+      d.cut = r.sm1 > r.pm1;
+      d.pad = 0;
+      srec[lt] = d;
+    }
+    group_sync(bar, L, whole);
+    for (int kk = w * SUBS; kk < nb; kk += nw * SUBS) {
+      const int k = kk + sub;
+      const bool live = k < nb;
+      const DegridRec r = srec[live ? k : kk];
+      float ar = 0.f, ai = 0.f, cr = 0.f, ci = 0.f;
+      if (live) {
+        const float2* gp = gcf + r.gcf;
+        const float2* sp = sg + r.q0;
+        const int wx = r.wx;
+        int j = sl / wx;
+        int i = sl - j * wx;
+        const int dj = SW / wx, di = SW - dj * wx;
 #pragma unroll 4
-    for (; j < wy;) {
-      const float2 c = __ldg(gp + j * pitch + i);
-      const float2 x = sp[j * A + i];
-      float pr, pi;
-      if (MODE == 0) {  // x * conj(c)
-        pr = x.x * c.x + x.y * c.y;
-        pi = x.y * c.x - x.x * c.y;
-      } else {  // -(x * c)
-        pr = -(x.x * c.x - x.y * c.y);
-        pi = -(x.x * c.y + x.y * c.x);
+        for (; j < r.wy;) {
+          const float2 c = __ldg(gp + j * r.pitch + i);
+          const float2 x = sp[j * A + i];
+          float pr, pi;
+          if (MODE == 0) {  // x * conj(c)
+            pr = x.x * c.x + x.y * c.y;
+            pi = x.y * c.x - x.x * c.y;
+          } else {  // -(x * c)
+            pr = -(x.x * c.x - x.y * c.y);
+            pi = -(x.x * c.y + x.y * c.x);
+          }
+          kahan(ar, cr, pr);
+          kahan(ai, ci, pi);
+          i += di;
+          j += dj;
+          if (i >= wx) {
+            i -= wx;
+            j++;
+          }
+        }
       }
-      two_sum(ar, cr, pr);
-      two_sum(ai, ci, pi);
-      i += di;
-      j += dj;
-      if (i >= wx) {
-        i -= wx;
-        j++;
-      }
-    }
-    ar += cr;
-    ai += ci;
+      ar -= cr;
+      ai -= ci;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      ar += __shfl_xor_sync(0xffffffffu, ar, o);
-      ai += __shfl_xor_sync(0xffffffffu, ai, o);
-    }
-    if (lane == 0) {
-      if (r.sm1 > r.pm1)
-        atomicAdd(pred + r.vis, make_float2(ar, ai));
-      else
-        pred[r.vis] = make_float2(ar, ai);
+      for (int o = SW / 2; o > 0; o >>= 1) {
+        ar += __shfl_xor_sync(0xffffffffu, ar, o);
+        ai += __shfl_xor_sync(0xffffffffu, ai, o);
+      }
+      if (live && sl == 0) {
+        if (r.cut)
+          atomicAdd(pred + r.vis, make_float2(ar, ai));
+        else
+          pred[r.vis] = make_float2(ar, ai);
+      }
     }
   }
 }
@@ -309,9 +354,18 @@ __global__ void __launch_bounds__(NT) k_degrid_tiled(TiledArgs a, const float2* 
     const int g = tid / ci.L;
     if (g < bd.n_items) {
       const int lt = tid - g * ci.L;
-      float2* sg = (float2*)(smem + (size_t)g * 8 * (size_t)ci.A * ci.A);
-      degrid_item<MODE>(a, a.items[bd.first_item + g], lt, ci.L, 1 + g, ci.L == NT, ci.A, sg, gcf,
-                        grid, pred);
+      unsigned char* base = smem + (size_t)g * degrid_group_bytes(ci.A, ci.L);
+      float2* sg = (float2*)base;
+      DegridRec* srec = (DegridRec*)(base + degrid_stage_bytes(ci.A));
+      const Item it = a.items[bd.first_item + g];
+      const bool whole = ci.L == NT;
+      // sub-warp width by piece size: <= 64 taps -> 8 lanes, <= 256 -> 16, else 32
+      if (ci.pmax <= 8)
+        degrid_item<MODE, 8>(a, it, lt, ci.L, 1 + g, whole, ci.A, sg, srec, gcf, grid, pred);
+      else if (ci.pmax <= 16)
+        degrid_item<MODE, 16>(a, it, lt, ci.L, 1 + g, whole, ci.A, sg, srec, gcf, grid, pred);
+      else
+        degrid_item<MODE, 32>(a, it, lt, ci.L, 1 + g, whole, ci.A, sg, srec, gcf, grid, pred);
     }
     __syncthreads();
   }
@@ -320,14 +374,14 @@ __global__ void __launch_bounds__(NT) k_degrid_tiled(TiledArgs a, const float2* 
 // ---------------------------------------------------------------- host side
 size_t tiled_smem_grid(const ClassInfo* cls, int n, int) {
   size_t m = 0;
-  for (int c = 0; c < n; c++)
-    m = std::max(m, (size_t)cls[c].G * (16 * (size_t)cls[c].A * cls[c].A + 24 * (size_t)cls[c].L));
+  for (int c = 0; c < n; c++) m = std::max(m, (size_t)cls[c].G * grid_group_bytes(cls[c].A, cls[c].L));
   return m;
 }
 
 size_t tiled_smem_degrid(const ClassInfo* cls, int n, int) {
   size_t m = 0;
-  for (int c = 0; c < n; c++) m = std::max(m, (size_t)cls[c].G * 8 * (size_t)cls[c].A * cls[c].A);
+  for (int c = 0; c < n; c++)
+    m = std::max(m, (size_t)cls[c].G * degrid_group_bytes(cls[c].A, cls[c].L));
   return m;
 }
 
@@ -343,30 +397,11 @@ int tiled_max_smem() {
   return cached;
 }
 
-static int residues_needed(const gb_plan* P) {
-  int R = 1;
-  for (int c = 0; c < P->n_classes; c++) {
-    const int pm = P->cls[c].pmax;
-    R = std::max(R, (pm * pm + P->cls[c].L - 1) / P->cls[c].L);
-  }
-  return R <= 1 ? 1 : R <= 2 ? 2 : R <= 4 ? 4 : 8;
-}
-
 typedef void (*GridFn)(TiledArgs, const float2*, const float2*, float2*);
 typedef void (*DegridFn)(TiledArgs, const float2*, const float2*, float2*);
 
-template <int NT>
-static GridFn grid_fn_nt(int R) {
-  switch (R) {
-    case 1: return k_grid_tiled<NT, 1, 4>;
-    case 2: return k_grid_tiled<NT, 2, 4>;
-    case 4: return k_grid_tiled<NT, 4, 2>;
-    default: return k_grid_tiled<NT, 8, 1>;
-  }
-}
-
-static GridFn grid_fn(int NT, int R) {
-  return NT == 128 ? grid_fn_nt<128>(R) : NT == 256 ? grid_fn_nt<256>(R) : grid_fn_nt<512>(R);
+static GridFn grid_fn(int NT) {
+  return NT == 128 ? k_grid_tiled<128> : NT == 256 ? k_grid_tiled<256> : k_grid_tiled<512>;
 }
 
 static DegridFn degrid_fn(int NT, int mode) {
@@ -382,7 +417,7 @@ static int set_smem_attr(const void* fn) {
 }
 
 int tiled_ctas_per_sm(const gb_plan* P, bool grid) {
-  const void* fn = grid ? (const void*)grid_fn(P->NT, residues_needed(P))
+  const void* fn = grid ? (const void*)grid_fn(P->NT)
                         : (const void*)degrid_fn(P->NT, 0);
   if (set_smem_attr(fn)) return 1;
   if (!grid) set_smem_attr((const void*)degrid_fn(P->NT, 1));
@@ -412,7 +447,7 @@ int launch_grid_tiled(gb_plan* P, const float* vis, const float* gcf, float* gri
   if (P->n_bundles == 0) return GB_OK;
   GB_CUDA_TRY(cudaMemsetAsync(P->d_queue, 0, sizeof(int32_t), s));
   const int blocks = std::min(P->n_bundles, sm_count() * P->ctas_per_sm_grid);
-  GridFn fn = grid_fn(P->NT, residues_needed(P));
+  GridFn fn = grid_fn(P->NT);
   fn<<<blocks, P->NT, P->smem_grid, s>>>(make_args(P), (const float2*)vis, (const float2*)gcf,
                                          (float2*)grid);
   GB_CUDA_TRY(cudaGetLastError());
@@ -440,11 +475,7 @@ int launch_grid_tiled_tables(const Bundle* bundles, int n_bundles, const Item* i
                              int NT, int T, int ext_x, int ext_y, int64_t pitch, size_t smem,
                              const float* vis, const float* gcf, float* grid, cudaStream_t s) {
   if (n_bundles <= 0) return GB_OK;
-  int R = 1;
-  for (int c = 0; c < n_classes; c++)
-    R = std::max(R, (cls[c].pmax * cls[c].pmax + cls[c].L - 1) / cls[c].L);
-  R = R <= 1 ? 1 : R <= 2 ? 2 : R <= 4 ? 4 : 8;
-  GridFn fn = grid_fn(NT, R);
+  GridFn fn = grid_fn(NT);
   int rc = set_smem_attr((const void*)fn);
   if (rc) return rc;
   int per_sm = 0;

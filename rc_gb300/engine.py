@@ -34,7 +34,7 @@ def _ptr(t):
 class Plan:
     def __init__(self, uvw, *, scale, grid_size, grid_shape, supports, gcf_offsets=None,
                  margin=None, w_range=None, plane=None, tile=0, threads=0, period_cap=0,
-                 stream=None):
+                 bundles_per_cta=0, stream=None):
         import torch
 
         assert uvw.is_cuda and uvw.dtype == torch.float64 and uvw.dim() == 2
@@ -57,6 +57,7 @@ class Plan:
         g.ext_x, g.ext_y, g.pitch = W, H, W
         g.n_planes = len(self.supports)
         g.tile, g.threads, g.period_cap = tile, threads, period_cap
+        g.bundles_per_cta = bundles_per_cta
         g.supports = self.supports.ctypes.data_as(C.POINTER(C.c_int32))
         g.gcf_offsets = self.gcf_offsets.ctypes.data_as(C.POINTER(C.c_int64))
         lo, hi = w_range if w_range is not None else (-np.inf, np.inf)
@@ -91,6 +92,7 @@ class Plan:
         assert vis.dtype == torch.complex64 and gcf.dtype == torch.complex64
         assert grid.dtype == torch.complex64 and grid.is_contiguous()
         assert grid.shape == self.grid_shape and vis.numel() == self.n
+        assert gcf.numel() >= self.gcf_len, "GCF array shorter than the plan's layout"
         _lib.check(self.L.gb_grid_f32(self.h, vis.data_ptr(), gcf.data_ptr(), grid.data_ptr(),
                                       _stream(stream)), "gb_grid_f32")
         return grid
@@ -100,6 +102,7 @@ class Plan:
 
         assert gcf.dtype == torch.complex64 and grid.dtype == torch.complex64
         assert grid.shape == self.grid_shape and grid.is_contiguous()
+        assert gcf.numel() >= self.gcf_len, "GCF array shorter than the plan's layout"
         if out is None:
             out = torch.empty(self.n, dtype=torch.complex64, device=grid.device)
         _lib.check(self.L.gb_degrid_f32(self.h, gcf.data_ptr(), grid.data_ptr(), out.data_ptr(),
@@ -112,6 +115,8 @@ class Plan:
 
         assert vis.dtype == torch.complex128 and gcf.dtype == torch.complex128
         assert grid.dtype == torch.complex128 and grid.is_contiguous()
+        assert grid.shape == self.grid_shape and vis.numel() == self.n
+        assert gcf.numel() >= self.gcf_len, "GCF array shorter than the plan's layout"
         _lib.check(self.L.gb_grid_f64(self.h, vis.data_ptr(), gcf.data_ptr(), grid.data_ptr(),
                                       _stream(stream)), "gb_grid_f64")
         return grid
@@ -119,6 +124,9 @@ class Plan:
     def degrid64(self, gcf, grid, out=None, mode=0, stream=None):
         import torch
 
+        assert gcf.dtype == torch.complex128 and grid.dtype == torch.complex128
+        assert grid.shape == self.grid_shape and grid.is_contiguous()
+        assert gcf.numel() >= self.gcf_len, "GCF array shorter than the plan's layout"
         if out is None:
             out = torch.empty(self.n, dtype=torch.complex128, device=grid.device)
         _lib.check(self.L.gb_degrid_f64(self.h, gcf.data_ptr(), grid.data_ptr(), out.data_ptr(),

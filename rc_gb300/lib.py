@@ -61,6 +61,7 @@ class Geometry(C.Structure):
         ("tile", C.c_int32),
         ("threads", C.c_int32),
         ("period_cap", C.c_int32),
+        ("bundles_per_cta", C.c_int32),
         ("supports", C.POINTER(C.c_int32)),
         ("gcf_offsets", C.POINTER(C.c_int64)),
         ("w_low", C.c_double),

@@ -39,7 +39,7 @@ def _geometry(sup, offs, G):
     g.margin = int(sup.max())
     g.ext_x = g.ext_y = g.pitch = G
     g.n_planes = len(sup)
-    g.tile = g.threads = g.period_cap = 0
+    g.tile = g.threads = g.period_cap = g.bundles_per_cta = 0
     g._sup = np.ascontiguousarray(sup, np.int32)
     g._offs = np.ascontiguousarray(offs, np.int64)
     g.supports = g._sup.ctypes.data_as(C.POINTER(C.c_int32))
