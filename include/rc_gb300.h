@@ -230,6 +230,24 @@ int gb_grid_f32_noalloc(const gb_geometry *geo, int64_t n_vis, const double *d_u
                         int64_t uvw_stride, const int32_t *d_plane, const float *d_vis,
                         const float *d_gcf, float *d_grid, void *stream);
 
+/* Image <-> grid transforms either side of the gridder (grid correction and
+ * centred FFT), replacing the reference's kern_fft / kern_ifft
+ * (MS6/kernel/cpu/gridding/fft1.cpp:29-57) and its GPU cuFFT + fftshift step
+ * (MS4/kernel/gpu/fft/cufftshift.cu:9-73).  For an even n x n real image x and
+ * a separable taper t (n values, NULL = none):
+ *   image_to_grid: grid = fftshift(FFT(ifftshift(x / (t_y t_x))))   (exp(-2 pi i))
+ *   grid_to_image: x    = Re[fftshift(IFFT(ifftshift(grid))) / (t_y t_x)]
+ * with IFFT unnormalised (exp(+2 pi i)), so grid_to_image is the exact adjoint
+ * of image_to_grid.  d_work: n*n complex scratch (not aliasing d_grid). */
+int gb_image_to_grid_f32(const float *d_image, const float *d_taper, int32_t n, float *d_grid,
+                         void *stream);
+int gb_grid_to_image_f32(const float *d_grid, const float *d_taper, int32_t n, float *d_work,
+                         float *d_image, void *stream);
+int gb_image_to_grid_f64(const double *d_image, const double *d_taper, int32_t n,
+                         double *d_grid, void *stream);
+int gb_grid_to_image_f64(const double *d_grid, const double *d_taper, int32_t n, double *d_work,
+                         double *d_image, void *stream);
+
 /* Zero `n_complex` complex64 grid elements (device). */
 int gb_grid_zero_f32(float *d_grid, int64_t n_complex, void *stream);
 

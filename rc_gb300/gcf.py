@@ -51,15 +51,19 @@ def plane_supports(w_low, w_high, n_planes, s_min=8, s_max=64):
     return np.array(sup, np.int32), centres
 
 
-def pswf(x, c):
-    """Order-0 prolate spheroidal angular function, normalised to 1 at x = 0,
-    zero for |x| >= 1."""
+def pswf(x, c, outside=0.0):
+    """Order-0 prolate spheroidal angular function, normalised to 1 at x = 0.
+    For |x| >= 1 it is `outside` (0: a kernel's support ends there), or, with
+    outside=None, its limit at the interval's edge (a taper sampled on
+    [-1, 1) keeps a non-zero first sample, so grid correction can divide)."""
     from scipy.special import pro_ang1
 
     x = np.asarray(x, np.float64)
     xc = np.clip(x, -1 + 1e-12, 1 - 1e-12)
     v = pro_ang1(0, 0, c, xc)[0] / pro_ang1(0, 0, c, 0.0)[0]
-    return np.where(np.abs(x) < 1.0, v, 0.0)
+    if outside is None:
+        return v
+    return np.where(np.abs(x) < 1.0, v, outside)
 
 
 def pswf_taper(max_support, width=7.0):
@@ -67,7 +71,7 @@ def pswf_taper(max_support, width=7.0):
     i in [-r, r)), for a uv-kernel of about `width` cells."""
     r = max_support // 2
     x = np.arange(-r, r + max_support % 2, dtype=np.float64) / r
-    return pswf(x, math.pi * width / 2.0)
+    return pswf(x, math.pi * width / 2.0, outside=None)
 
 
 def pswf_uv_gcf(support=8, width=7, over=OVER):

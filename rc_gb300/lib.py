@@ -97,6 +97,10 @@ SIGNATURES = {
                                   C.POINTER(C.c_int64), C.c_int32, C.c_double, _VP, _VP, _VP,
                                   _VP]),
     "gb_grid_zero_f32": (C.c_int, [_VP, C.c_int64, _VP]),
+    "gb_image_to_grid_f32": (C.c_int, [_VP, _VP, C.c_int32, _VP, _VP]),
+    "gb_grid_to_image_f32": (C.c_int, [_VP, _VP, C.c_int32, _VP, _VP, _VP]),
+    "gb_image_to_grid_f64": (C.c_int, [_VP, _VP, C.c_int32, _VP, _VP]),
+    "gb_grid_to_image_f64": (C.c_int, [_VP, _VP, C.c_int32, _VP, _VP, _VP]),
     "gb_grid_f32_noalloc": (C.c_int, [C.POINTER(Geometry), C.c_int64, _VP, C.c_int64, _VP, _VP,
                                       _VP, _VP, _VP]),
 }

@@ -113,6 +113,23 @@ def predict(uvw, l, m, flux, rng, noise=0.01, chunk=1 << 20):
     return out
 
 
+def sky_image(n, rng, n_blobs=20, sigma=(1.0, 5.0), flux=(0.1, 10.0), margin=0.25):
+    """Real float32 n x n sky of Gaussian blobs (sigma uniform in px, peak
+    log-uniform) on a zero background, centres within the inner 1 - 2*margin."""
+    img = np.zeros((n, n), np.float64)
+    yy, xx = np.mgrid[0:n, 0:n]
+    lo, hi = margin * n, (1 - margin) * n
+    for _ in range(n_blobs):
+        cy, cx = rng.uniform(lo, hi, 2)
+        s = rng.uniform(*sigma)
+        a = np.exp(rng.uniform(np.log(flux[0]), np.log(flux[1])))
+        y0, y1 = int(max(0, cy - 6 * s)), int(min(n, cy + 6 * s + 1))
+        x0, x1 = int(max(0, cx - 6 * s)), int(min(n, cx + 6 * s + 1))
+        img[y0:y1, x0:x1] += a * np.exp(-((yy[y0:y1, x0:x1] - cy) ** 2 +
+                                          (xx[y0:y1, x0:x1] - cx) ** 2) / (2 * s * s))
+    return img.astype(np.float32)
+
+
 def _finish(name, rng, uvw_m, freqs, grid_size, n_planes, s_min, s_max):
     """metres -> wavelengths per channel, sky, scale, w-planes."""
     from .gcf import plane_supports
