@@ -195,6 +195,39 @@ int gb_gcf_generate(int32_t n_planes, const double *w_planes, const int32_t *sup
                     const int64_t *gcf_offsets, int32_t max_support, double t2,
                     const double *d_taper, double *d_gcf64, float *d_gcf32, void *stream);
 
+/* Batched FP32 gridding / degridding: up to GB_MAX_BATCH grids (channels,
+ * facets, data sets; any sizes and w-plane sets) in ONE persistent launch fed
+ * by one device work queue, longest work first.  The reference runs such units
+ * as separate actors, one kernel call per (tile, w-bin) region
+ * (MS6/programs/continuum.hs:134-193).  Every member is planned like
+ * gb_plan_create (all members must use the same tile and threads); the GCF
+ * array is shared (each member's gcf_offsets index into it).  The execute
+ * calls take host arrays of n_members device pointers and capture into a CUDA
+ * graph. */
+#define GB_MAX_BATCH 96
+typedef struct gb_batch gb_batch;
+typedef struct gb_batch_member {
+  gb_geometry geo;
+  int64_t n_vis;
+  const double *d_uvw;
+  int64_t uvw_stride;
+  const int32_t *d_plane; /* optional, as for gb_plan_create */
+} gb_batch_member;
+int gb_batch_create(int32_t n_members, const gb_batch_member *members, void *stream,
+                    gb_batch **out);
+int gb_batch_destroy(gb_batch *batch);
+/* [0] visibilities kept, [1] taps, [2] items, [3] bundles, [4] tile, [5] members, [6] threads */
+int gb_batch_stats(const gb_batch *batch, int64_t *stats7);
+int gb_batch_grid_f32(gb_batch *batch, const float *const *d_vis, const float *d_gcf,
+                      float *const *d_grids, void *stream);
+int gb_batch_degrid_f32(gb_batch *batch, const float *d_gcf, const float *const *d_grids,
+                        float *const *d_preds, int32_t mode, void *stream);
+/* The plain FP64 path over the members (one launch per member, complex128). */
+int gb_batch_grid_f64(gb_batch *batch, const double *const *d_vis, const double *d_gcf,
+                      double *const *d_grids, void *stream);
+int gb_batch_degrid_f64(gb_batch *batch, const double *d_gcf, const double *const *d_grids,
+                        double *const *d_preds, int32_t mode, void *stream);
+
 /* Allocation-free gridding.  No counterpart in the reference.
  *
  * For callers that cannot call cudaMalloc: code running inside a host
@@ -204,7 +237,7 @@ int gb_gcf_generate(int32_t n_planes, const double *w_planes, const int32_t *sup
  * gb_plan_create + gb_grid_f32 + gb_plan_destroy do together (grid += G vis,
  * same FP32 tiled kernel, same tolerance) for one batch of visibilities, and
  * calls no cudaMalloc, cudaFree or allocating library routine: its working
- * memory is one static device array of GB_NOALLOC_SCRATCH_BYTES (7 MiB),
+ * memory is one static device array of GB_NOALLOC_SCRATCH_BYTES (8 MiB),
  * which every GPU that loads this library holds until the process exits.
  * The caller passes inputs and the output grid (device pointers, as for
  * gb_plan_create / gb_grid_f32).
@@ -225,7 +258,7 @@ int gb_gcf_generate(int32_t n_planes, const double *w_planes, const int32_t *sup
 #define GB_NOALLOC_MAX_PIECES (1 << 18)
 #define GB_NOALLOC_MAX_BINS (1 << 16)
 #define GB_NOALLOC_MAX_PLANES 256
-#define GB_NOALLOC_SCRATCH_BYTES (7 << 20)
+#define GB_NOALLOC_SCRATCH_BYTES (8 << 20)
 int gb_grid_f32_noalloc(const gb_geometry *geo, int64_t n_vis, const double *d_uvw,
                         int64_t uvw_stride, const int32_t *d_plane, const float *d_vis,
                         const float *d_gcf, float *d_grid, void *stream);

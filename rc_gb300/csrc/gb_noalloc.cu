@@ -159,6 +159,8 @@ __global__ void __launch_bounds__(1024) k_na_tables(const int32_t* __restrict__ 
     B.first_item = cls_first[c] + j * nc.G[c];
     B.n_items = (int16_t)min(nc.G[c], n_c - j * nc.G[c]);
     B.cls = (int16_t)c;
+    B.grid = 0;
+    B.pad = 0;
     bundles[b] = B;
   }
   if (tid == 0) counters[kCntBundles] = total;

@@ -174,10 +174,43 @@ static int dalloc(T** p, size_t n) {
   return GB_OK;
 }
 
-struct HostItem {
-  Item it;
-  double cost;
-};
+void make_bundles(const std::vector<HostItem>& items, const ClassInfo* cls, int n_classes,
+                  std::vector<Item>& it_out, std::vector<Bundle>& b_out) {
+  struct HB {
+    Bundle b;
+    double cost;
+  };
+  std::vector<HB> bundles;
+  int max_grid = 0;
+  for (const auto& h : items) max_grid = std::max(max_grid, h.grid);
+  it_out.clear();
+  for (int c = 0; c < n_classes; c++) {
+    for (int g = 0; g <= max_grid; g++) {
+      std::vector<HostItem> ci;
+      for (const auto& h : items)
+        if (h.it.cls == c && h.grid == g) ci.push_back(h);
+      if (ci.empty()) continue;
+      std::stable_sort(ci.begin(), ci.end(),
+                       [](const HostItem& a, const HostItem& b) { return a.cost > b.cost; });
+      const int G = cls[c].G;
+      for (size_t i = 0; i < ci.size(); i += G) {
+        HB hb;
+        hb.b.first_item = (int32_t)it_out.size();
+        hb.b.n_items = (int16_t)std::min<size_t>(G, ci.size() - i);
+        hb.b.cls = (int16_t)c;
+        hb.b.grid = g;
+        hb.b.pad = 0;
+        hb.cost = ci[i].cost;
+        for (int k = 0; k < hb.b.n_items; k++) it_out.push_back(ci[i + k].it);
+        bundles.push_back(hb);
+      }
+    }
+  }
+  std::stable_sort(bundles.begin(), bundles.end(),
+                   [](const HB& a, const HB& b) { return a.cost > b.cost; });
+  b_out.clear();
+  for (auto& hb : bundles) b_out.push_back(hb.b);
+}
 
 static int build_plan(gb_plan* P, const gb_geometry* geo, int64_t n_vis, const double* d_uvw,
                       int64_t uvw_stride, const int32_t* d_plane_in, cudaStream_t s) {
@@ -383,37 +416,26 @@ static int build_plan(gb_plan* P, const gb_geometry* geo, int64_t n_vis, const d
     }
   }
   P->tiles_used = tiles_used;
-  // bundles: per class, items by decreasing cost, G at a time; then all
-  // bundles by decreasing cost (longest first).
+  for (auto& h : items) h.grid = 0;
   std::vector<Item> it_sorted;
-  struct HB {
-    Bundle b;
-    double cost;
-  };
-  std::vector<HB> bundles;
-  for (int c = 0; c < P->n_classes; c++) {
-    std::vector<HostItem> ci;
-    for (auto& h : items)
-      if (h.it.cls == c) ci.push_back(h);
-    std::stable_sort(ci.begin(), ci.end(),
-                     [](const HostItem& a, const HostItem& b) { return a.cost > b.cost; });
-    const int G = P->cls[c].G;
-    for (size_t i = 0; i < ci.size(); i += G) {
-      HB hb;
-      hb.b.first_item = (int32_t)it_sorted.size();
-      hb.b.n_items = (int16_t)std::min<size_t>(G, ci.size() - i);
-      hb.b.cls = (int16_t)c;
-      hb.cost = ci[i].cost;
-      for (int g = 0; g < hb.b.n_items; g++) it_sorted.push_back(ci[i + g].it);
-      bundles.push_back(hb);
-    }
-  }
-  std::stable_sort(bundles.begin(), bundles.end(),
-                   [](const HB& a, const HB& b) { return a.cost > b.cost; });
   std::vector<Bundle> bvec;
-  for (auto& hb : bundles) bvec.push_back(hb.b);
+  make_bundles(items, P->cls, P->n_classes, it_sorted, bvec);
   P->n_items = (int)it_sorted.size();
   P->n_bundles = (int)bvec.size();
+  // host copy of the items in device order, for batched launches
+  P->host_items.clear();
+  {
+    std::vector<HostItem> by_key = items;
+    // it_sorted is a permutation of items: recover each item's cost by its record range
+    std::sort(by_key.begin(), by_key.end(),
+              [](const HostItem& a, const HostItem& b) { return a.it.start < b.it.start; });
+    for (const Item& it : it_sorted) {
+      auto f = std::lower_bound(by_key.begin(), by_key.end(), it.start,
+                                [](const HostItem& a, int32_t v) { return a.it.start < v; });
+      HostItem h = *f;
+      P->host_items.push_back(h);
+    }
+  }
 
   // ---- fill
   if ((rc = dalloc(&P->d_recs, P->n_recs)) || (rc = dalloc(&P->d_items, P->n_items)) ||

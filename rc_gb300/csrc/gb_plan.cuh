@@ -53,9 +53,19 @@ struct __align__(16) Item {
 };
 static_assert(sizeof(Item) == 16, "Item must be 16 bytes");
 
-struct __align__(8) Bundle {
+struct __align__(16) Bundle {
   int32_t first_item;
   int16_t n_items, cls;
+  int32_t grid;  // slot of the grid (and visibility array) in a batched launch
+  int32_t pad;
+};
+static_assert(sizeof(Bundle) == 16, "Bundle must be 16 bytes");
+
+// Item with its modelled cost and grid slot, kept on the host to form bundles.
+struct HostItem {
+  Item it;
+  double cost;
+  int grid;
 };
 
 // One thread-group class: L threads per group, G groups per CTA, region edge A.
@@ -77,6 +87,20 @@ __host__ __device__ inline size_t degrid_group_bytes(int A, int L) {
 }
 
 constexpr int kMaxClasses = 4;
+
+// Per-grid pointers and geometry of a (batched) launch, passed by value as a
+// __grid_constant__ kernel parameter.  vis: the visibilities (gridding input)
+// or the predictions (degridding output) of that grid's plan.
+constexpr int kMaxGrids = 96;
+struct GridSlot {
+  float2* grid;
+  float2* vis;
+  int64_t pitch;
+  int32_t ext_x, ext_y;
+};
+struct GridPtrs {
+  GridSlot s[kMaxGrids];
+};
 
 struct PlaneInfo {
   int32_t S, P, k, rank;
@@ -115,9 +139,15 @@ struct gb_plan {
   int n_items = 0, n_bundles = 0;
   int64_t kept = 0, taps = 0, tiles_used = 0;
   bool own_plane = true;
+  std::vector<gb::HostItem> host_items;  // in d_items order (grid slot 0)
 };
 
 namespace gb {
+// Bundles from items: grouped by (class, grid), by decreasing cost, up to
+// cls[c].G items each; all bundles then by decreasing cost (longest first).
+// it_out receives the items in bundle order.
+void make_bundles(const std::vector<HostItem>& items, const ClassInfo* cls, int n_classes,
+                  std::vector<Item>& it_out, std::vector<Bundle>& b_out);
 int launch_grid_plain64(const gb_plan* plan, const double* vis, const double* gcf, double* grid,
                         cudaStream_t s);
 int launch_degrid_plain64(const gb_plan* plan, const double* gcf, const double* grid,
@@ -134,6 +164,11 @@ int launch_grid_tiled_tables(const Bundle* bundles, int n_bundles, const Item* i
                              const Rec* recs, int32_t* queue, const ClassInfo* cls, int n_classes,
                              int NT, int T, int ext_x, int ext_y, int64_t pitch, size_t smem,
                              const float* vis, const float* gcf, float* grid, cudaStream_t s);
+int launch_tiled_batch(bool grid_mode, int mode, int NT, size_t smem, int ctas_per_sm,
+                       const Bundle* bundles, int n_bundles, const Item* items, const Rec* recs,
+                       int32_t* queue, const ClassInfo* cls, int n_classes, int T,
+                       const GridPtrs& gp, const float* gcf, cudaStream_t s);
+int tiled_ctas_per_sm_for(int NT, bool grid, size_t smem);
 // Resident CTAs per SM of the tiled grid (or degrid) kernel for this plan.
 int tiled_ctas_per_sm(const gb_plan* plan, bool grid);
 }  // namespace gb

@@ -26,6 +26,7 @@
 // compensation and a warp-shuffle reduction.  A visibility whose footprint was cut into
 // several pieces accumulates them with float2 atomics; otherwise a plain store.
 #include <algorithm>
+#include <cstring>
 #include <mutex>
 
 #include "gb_common.cuh"
@@ -41,8 +42,7 @@ struct TiledArgs {
   int32_t* queue;
   ClassInfo cls[kMaxClasses];
   int32_t n_bundles;
-  int32_t T, ext_x, ext_y;
-  int64_t pitch;
+  int32_t T;
 };
 
 __device__ __forceinline__ void group_sync(int id, int n, bool whole_cta) {
@@ -157,9 +157,9 @@ __device__ __forceinline__ void grid_run(int k, int e, int lt, int L, int A,
 __device__ __forceinline__ void grid_item(const TiledArgs& a, const Item& it, int lt, int L,
                                           int bar, bool whole, int A, float4* __restrict__ acc,
                                           GridRec* __restrict__ srec, float2* __restrict__ svis,
-                                          const float2* __restrict__ vis,
-                                          const float2* __restrict__ gcf,
-                                          float2* __restrict__ grid) {
+                                          const GridSlot& gs, const float2* __restrict__ gcf) {
+  const float2* __restrict__ vis = gs.vis;
+  float2* __restrict__ grid = gs.grid;
   const int AA = A * A;
   for (int q = lt; q < AA; q += L) acc[q] = make_float4(0.f, 0.f, 0.f, 0.f);
   int curP = -1;
@@ -211,16 +211,16 @@ __device__ __forceinline__ void grid_item(const TiledArgs& a, const Item& it, in
     if (s.x != 0.f || s.y != 0.f || s.z != 0.f || s.w != 0.f) {
       const int py = q / A, px = q - py * A;
       const int gx = x0 + px, gy = y0 + py;
-      if (gx < a.ext_x && gy < a.ext_y)
-        atomicAdd(grid + (int64_t)gy * a.pitch + gx, make_float2(s.x - s.z, s.y - s.w));
+      if (gx < gs.ext_x && gy < gs.ext_y)
+        atomicAdd(grid + (int64_t)gy * gs.pitch + gx, make_float2(s.x - s.z, s.y - s.w));
     }
   }
 }
 
 template <int NT>
-__global__ void __launch_bounds__(NT) k_grid_tiled(TiledArgs a, const float2* __restrict__ vis,
-                                                   const float2* __restrict__ gcf,
-                                                   float2* __restrict__ grid) {
+__global__ void __launch_bounds__(NT) k_grid_tiled(const __grid_constant__ TiledArgs a,
+                                                   const __grid_constant__ GridPtrs gp,
+                                                   const float2* __restrict__ gcf) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ int s_b;
   const int tid = threadIdx.x;
@@ -240,7 +240,7 @@ __global__ void __launch_bounds__(NT) k_grid_tiled(TiledArgs a, const float2* __
       GridRec* srec = (GridRec*)(base + 16 * (size_t)AA);
       float2* svis = (float2*)(base + 16 * (size_t)AA + 32 * (size_t)ci.L);
       grid_item(a, a.items[bd.first_item + g], lt, ci.L, 1 + g, ci.L == NT, ci.A, acc, srec,
-                svis, vis, gcf, grid);
+                svis, gp.s[bd.grid], gcf);
     }
     __syncthreads();
   }
@@ -253,17 +253,17 @@ __global__ void __launch_bounds__(NT) k_grid_tiled(TiledArgs a, const float2* __
 template <int MODE, int SW>
 __device__ __forceinline__ void degrid_item(const TiledArgs& a, const Item& it, int lt, int L,
                                             int bar, bool whole, int A, float2* __restrict__ sg,
-                                            DegridRec* __restrict__ srec,
-                                            const float2* __restrict__ gcf,
-                                            const float2* __restrict__ grid,
-                                            float2* __restrict__ pred) {
+                                            DegridRec* __restrict__ srec, const GridSlot& gs,
+                                            const float2* __restrict__ gcf) {
+  const float2* __restrict__ grid = gs.grid;
+  float2* __restrict__ pred = gs.vis;
   const int AA = A * A;
   const int x0 = it.tile_x * a.T, y0 = it.tile_y * a.T;
   for (int q = lt; q < AA; q += L) {
     const int py = q / A, px = q - py * A;
     const int gx = x0 + px, gy = y0 + py;
-    sg[q] = (gx < a.ext_x && gy < a.ext_y) ? grid[(int64_t)gy * a.pitch + gx]
-                                           : make_float2(0.f, 0.f);
+    sg[q] = (gx < gs.ext_x && gy < gs.ext_y) ? grid[(int64_t)gy * gs.pitch + gx]
+                                             : make_float2(0.f, 0.f);
   }
   constexpr int SUBS = 32 / SW;
   const int nw = L >> 5, w = lt >> 5, lane = lt & 31;
@@ -338,9 +338,9 @@ __device__ __forceinline__ void degrid_item(const TiledArgs& a, const Item& it, 
 }
 
 template <int NT, int MODE>
-__global__ void __launch_bounds__(NT) k_degrid_tiled(TiledArgs a, const float2* __restrict__ gcf,
-                                                     const float2* __restrict__ grid,
-                                                     float2* __restrict__ pred) {
+__global__ void __launch_bounds__(NT) k_degrid_tiled(const __grid_constant__ TiledArgs a,
+                                                     const __grid_constant__ GridPtrs gp,
+                                                     const float2* __restrict__ gcf) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ int s_b;
   const int tid = threadIdx.x;
@@ -361,11 +361,11 @@ __global__ void __launch_bounds__(NT) k_degrid_tiled(TiledArgs a, const float2* 
       const bool whole = ci.L == NT;
       // sub-warp width by piece size: <= 64 taps -> 8 lanes, <= 256 -> 16, else 32
       if (ci.pmax <= 8)
-        degrid_item<MODE, 8>(a, it, lt, ci.L, 1 + g, whole, ci.A, sg, srec, gcf, grid, pred);
+        degrid_item<MODE, 8>(a, it, lt, ci.L, 1 + g, whole, ci.A, sg, srec, gp.s[bd.grid], gcf);
       else if (ci.pmax <= 16)
-        degrid_item<MODE, 16>(a, it, lt, ci.L, 1 + g, whole, ci.A, sg, srec, gcf, grid, pred);
+        degrid_item<MODE, 16>(a, it, lt, ci.L, 1 + g, whole, ci.A, sg, srec, gp.s[bd.grid], gcf);
       else
-        degrid_item<MODE, 32>(a, it, lt, ci.L, 1 + g, whole, ci.A, sg, srec, gcf, grid, pred);
+        degrid_item<MODE, 32>(a, it, lt, ci.L, 1 + g, whole, ci.A, sg, srec, gp.s[bd.grid], gcf);
     }
     __syncthreads();
   }
@@ -397,8 +397,8 @@ int tiled_max_smem() {
   return cached;
 }
 
-typedef void (*GridFn)(TiledArgs, const float2*, const float2*, float2*);
-typedef void (*DegridFn)(TiledArgs, const float2*, const float2*, float2*);
+typedef void (*GridFn)(const TiledArgs, const GridPtrs, const float2*);
+typedef void (*DegridFn)(const TiledArgs, const GridPtrs, const float2*);
 
 static GridFn grid_fn(int NT) {
   return NT == 128 ? k_grid_tiled<128> : NT == 256 ? k_grid_tiled<256> : k_grid_tiled<512>;
@@ -436,10 +436,19 @@ static TiledArgs make_args(const gb_plan* P) {
   for (int c = 0; c < kMaxClasses; c++) a.cls[c] = P->cls[c];
   a.n_bundles = P->n_bundles;
   a.T = P->T;
-  a.ext_x = P->dev.ext_x;
-  a.ext_y = P->dev.ext_y;
-  a.pitch = P->dev.pitch;
   return a;
+}
+
+static GridPtrs one_grid(const float* grid, const float* vis, int ext_x, int ext_y,
+                         int64_t pitch) {
+  GridPtrs gp;
+  memset(&gp, 0, sizeof(gp));
+  gp.s[0].grid = (float2*)grid;
+  gp.s[0].vis = (float2*)vis;
+  gp.s[0].pitch = pitch;
+  gp.s[0].ext_x = ext_x;
+  gp.s[0].ext_y = ext_y;
+  return gp;
 }
 
 int launch_grid_tiled(gb_plan* P, const float* vis, const float* gcf, float* grid,
@@ -448,8 +457,9 @@ int launch_grid_tiled(gb_plan* P, const float* vis, const float* gcf, float* gri
   GB_CUDA_TRY(cudaMemsetAsync(P->d_queue, 0, sizeof(int32_t), s));
   const int blocks = std::min(P->n_bundles, sm_count() * P->ctas_per_sm_grid);
   GridFn fn = grid_fn(P->NT);
-  fn<<<blocks, P->NT, P->smem_grid, s>>>(make_args(P), (const float2*)vis, (const float2*)gcf,
-                                         (float2*)grid);
+  fn<<<blocks, P->NT, P->smem_grid, s>>>(
+      make_args(P), one_grid(grid, vis, P->dev.ext_x, P->dev.ext_y, P->dev.pitch),
+      (const float2*)gcf);
   GB_CUDA_TRY(cudaGetLastError());
   return GB_OK;
 }
@@ -461,8 +471,9 @@ int launch_degrid_tiled(gb_plan* P, const float* gcf, const float* grid, float* 
   GB_CUDA_TRY(cudaMemsetAsync(P->d_queue + 1, 0, sizeof(int32_t), s));
   const int blocks = std::min(P->n_bundles, sm_count() * P->ctas_per_sm_degrid);
   DegridFn fn = degrid_fn(P->NT, mode);
-  fn<<<blocks, P->NT, P->smem_degrid, s>>>(make_args(P), (const float2*)gcf, (const float2*)grid,
-                                           (float2*)pred);
+  fn<<<blocks, P->NT, P->smem_degrid, s>>>(
+      make_args(P), one_grid(grid, pred, P->dev.ext_x, P->dev.ext_y, P->dev.pitch),
+      (const float2*)gcf);
   GB_CUDA_TRY(cudaGetLastError());
   return GB_OK;
 }
@@ -489,13 +500,48 @@ int launch_grid_tiled_tables(const Bundle* bundles, int n_bundles, const Item* i
   for (int c = 0; c < kMaxClasses; c++) a.cls[c] = c < n_classes ? cls[c] : ClassInfo{64, 1, 1, 1};
   a.n_bundles = n_bundles;
   a.T = T;
-  a.ext_x = ext_x;
-  a.ext_y = ext_y;
-  a.pitch = pitch;
   GB_CUDA_TRY(cudaMemsetAsync(queue, 0, sizeof(int32_t), s));
-  fn<<<blocks, NT, smem, s>>>(a, (const float2*)vis, (const float2*)gcf, (float2*)grid);
+  fn<<<blocks, NT, smem, s>>>(a, one_grid(grid, vis, ext_x, ext_y, pitch), (const float2*)gcf);
   GB_CUDA_TRY(cudaGetLastError());
   return GB_OK;
+}
+
+// Batched launches: one persistent kernel over the bundles of several grids.
+int launch_tiled_batch(bool grid_mode, int mode, int NT, size_t smem, int ctas_per_sm,
+                       const Bundle* bundles, int n_bundles, const Item* items, const Rec* recs,
+                       int32_t* queue, const ClassInfo* cls, int n_classes, int T,
+                       const GridPtrs& gp, const float* gcf, cudaStream_t s) {
+  if (n_bundles <= 0) return GB_OK;
+  TiledArgs a;
+  a.bundles = bundles;
+  a.items = items;
+  a.recs = recs;
+  a.queue = queue;
+  for (int c = 0; c < kMaxClasses; c++) a.cls[c] = c < n_classes ? cls[c] : ClassInfo{64, 1, 1, 1};
+  a.n_bundles = n_bundles;
+  a.T = T;
+  const int blocks = std::min(n_bundles, sm_count() * std::max(1, ctas_per_sm));
+  // queue: the two work-queue heads (the grid kernel uses [0], degrid [1])
+  GB_CUDA_TRY(cudaMemsetAsync(queue + (grid_mode ? 0 : 1), 0, sizeof(int32_t), s));
+  if (grid_mode) {
+    GridFn fn = grid_fn(NT);
+    fn<<<blocks, NT, smem, s>>>(a, gp, (const float2*)gcf);
+  } else {
+    DegridFn fn = degrid_fn(NT, mode);
+    fn<<<blocks, NT, smem, s>>>(a, gp, (const float2*)gcf);
+  }
+  GB_CUDA_TRY(cudaGetLastError());
+  return GB_OK;
+}
+
+// Occupancy of the batched kernels (sets their shared-memory limit first).
+int tiled_ctas_per_sm_for(int NT, bool grid, size_t smem) {
+  const void* fn = grid ? (const void*)grid_fn(NT) : (const void*)degrid_fn(NT, 0);
+  if (set_smem_attr(fn)) return 1;
+  if (!grid) set_smem_attr((const void*)degrid_fn(NT, 1));
+  int n = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, NT, smem);
+  return n > 0 ? n : 1;
 }
 
 }  // namespace gb

@@ -143,3 +143,111 @@ class Plan:
             self.close()
         except Exception:
             pass
+
+
+class Batch:
+    """Several grids in one persistent launch (gb_batch_*).
+
+    members: list of dicts with the Plan keyword arguments (uvw, scale,
+    grid_size, grid_shape, supports, gcf_offsets, margin, w_range, plane);
+    tile/threads/period_cap/bundles_per_cta apply to all.  The GCF array is
+    shared: every member's gcf_offsets index into the one passed to grid()."""
+
+    def __init__(self, members, *, tile=0, threads=0, period_cap=0, bundles_per_cta=0,
+                 stream=None):
+        import torch
+
+        self.L = _lib.load()
+        n = len(members)
+        assert 1 <= n <= _lib.MAX_BATCH
+        arr = (_lib.BatchMember * n)()
+        self._keep = []
+        self.shapes, self.ns, self.gcf_len = [], [], 0
+        for i, m in enumerate(members):
+            uvw = m["uvw"]
+            assert uvw.is_cuda and uvw.dtype == torch.float64 and uvw.stride(1) == 1
+            sup = np.ascontiguousarray(m["supports"], np.int32)
+            offs = m.get("gcf_offsets")
+            if offs is None:
+                offs, total = layout(sup)
+            else:
+                total = int(max(o + 64 * s * s for o, s in zip(offs, sup)))
+            offs = np.ascontiguousarray(offs, np.int64)
+            self.gcf_len = max(self.gcf_len, total)
+            H, W = m["grid_shape"]
+            g = arr[i].geo
+            g.scale = float(m["scale"])
+            g.grid_size = int(m["grid_size"])
+            g.margin = int(sup.max() if m.get("margin") is None else m["margin"])
+            g.ext_x, g.ext_y, g.pitch = W, H, W
+            g.n_planes = len(sup)
+            g.tile, g.threads, g.period_cap = tile, threads, period_cap
+            g.bundles_per_cta = bundles_per_cta
+            g.supports = sup.ctypes.data_as(C.POINTER(C.c_int32))
+            g.gcf_offsets = offs.ctypes.data_as(C.POINTER(C.c_int64))
+            lo, hi = m.get("w_range") or (-np.inf, np.inf)
+            g.w_low, g.w_high = float(lo), float(hi)
+            arr[i].n_vis = uvw.shape[0]
+            arr[i].d_uvw = uvw.data_ptr()
+            arr[i].uvw_stride = uvw.stride(0)
+            arr[i].d_plane = _ptr(m.get("plane"))
+            self._keep += [uvw, sup, offs, m.get("plane")]
+            self.shapes.append((H, W))
+            self.ns.append(uvw.shape[0])
+        h = C.c_void_p()
+        _lib.check(self.L.gb_batch_create(n, arr, _stream(stream), C.byref(h)), "gb_batch_create")
+        self.h = h
+        self.n = n
+
+    def stats(self):
+        st = (C.c_int64 * 7)()
+        _lib.check(self.L.gb_batch_stats(self.h, st), "gb_batch_stats")
+        return dict(zip(["kept", "taps", "items", "bundles", "tile", "members", "threads"],
+                        list(st)))
+
+    def _ptrs(self, ts):
+        return (C.c_void_p * self.n)(*[t.data_ptr() for t in ts])
+
+    def grid(self, vis_list, gcf, grids, stream=None):
+        assert len(vis_list) == self.n and len(grids) == self.n
+        assert gcf.numel() >= self.gcf_len
+        for v, g, shp, nv in zip(vis_list, grids, self.shapes, self.ns):
+            assert v.numel() == nv and tuple(g.shape) == shp and g.is_contiguous()
+        _lib.check(self.L.gb_batch_grid_f32(self.h, self._ptrs(vis_list), gcf.data_ptr(),
+                                            self._ptrs(grids), _stream(stream)),
+                   "gb_batch_grid_f32")
+        return grids
+
+    def degrid(self, gcf, grids, preds=None, mode=0, stream=None):
+        import torch
+
+        assert len(grids) == self.n and gcf.numel() >= self.gcf_len
+        if preds is None:
+            preds = [torch.empty(nv, dtype=torch.complex64, device=gcf.device) for nv in self.ns]
+        _lib.check(self.L.gb_batch_degrid_f32(self.h, gcf.data_ptr(), self._ptrs(grids),
+                                              self._ptrs(preds), int(mode), _stream(stream)),
+                   "gb_batch_degrid_f32")
+        return preds
+
+    def grid64(self, vis_list, gcf, grids, stream=None):
+        _lib.check(self.L.gb_batch_grid_f64(self.h, self._ptrs(vis_list), gcf.data_ptr(),
+                                            self._ptrs(grids), _stream(stream)),
+                   "gb_batch_grid_f64")
+        return grids
+
+    def degrid64(self, gcf, grids, preds, mode=0, stream=None):
+        _lib.check(self.L.gb_batch_degrid_f64(self.h, gcf.data_ptr(), self._ptrs(grids),
+                                              self._ptrs(preds), int(mode), _stream(stream)),
+                   "gb_batch_degrid_f64")
+        return preds
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.gb_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

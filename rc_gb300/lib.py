@@ -69,6 +69,18 @@ class Geometry(C.Structure):
     ]
 
 
+class BatchMember(C.Structure):
+    _fields_ = [
+        ("geo", Geometry),
+        ("n_vis", C.c_int64),
+        ("d_uvw", C.c_void_p),
+        ("uvw_stride", C.c_int64),
+        ("d_plane", C.c_void_p),
+    ]
+
+
+MAX_BATCH = 96
+
 # every exported symbol of include/rc_gb300.h: name -> (restype, argtypes)
 _VP = C.c_void_p
 _BP = C.POINTER(BufferT)
@@ -97,6 +109,15 @@ SIGNATURES = {
                                   C.POINTER(C.c_int64), C.c_int32, C.c_double, _VP, _VP, _VP,
                                   _VP]),
     "gb_grid_zero_f32": (C.c_int, [_VP, C.c_int64, _VP]),
+    "gb_batch_create": (C.c_int, [C.c_int32, C.POINTER(BatchMember), _VP, C.POINTER(_VP)]),
+    "gb_batch_destroy": (C.c_int, [_VP]),
+    "gb_batch_stats": (C.c_int, [_VP, C.POINTER(C.c_int64)]),
+    "gb_batch_grid_f32": (C.c_int, [_VP, C.POINTER(_VP), _VP, C.POINTER(_VP), _VP]),
+    "gb_batch_degrid_f32": (C.c_int, [_VP, _VP, C.POINTER(_VP), C.POINTER(_VP), C.c_int32,
+                                      _VP]),
+    "gb_batch_grid_f64": (C.c_int, [_VP, C.POINTER(_VP), _VP, C.POINTER(_VP), _VP]),
+    "gb_batch_degrid_f64": (C.c_int, [_VP, _VP, C.POINTER(_VP), C.POINTER(_VP), C.c_int32,
+                                      _VP]),
     "gb_image_to_grid_f32": (C.c_int, [_VP, _VP, C.c_int32, _VP, _VP]),
     "gb_grid_to_image_f32": (C.c_int, [_VP, _VP, C.c_int32, _VP, _VP, _VP]),
     "gb_image_to_grid_f64": (C.c_int, [_VP, _VP, C.c_int32, _VP, _VP]),

@@ -155,6 +155,47 @@ def _finish(name, rng, uvw_m, freqs, grid_size, n_planes, s_min, s_max):
                        supports, centres, low, high, int(supports.max()), n_bl, n_t, len(freqs))
 
 
+def config3(seed: int | None = None, n_t: int = 216, n_ch: int = 64, n_facets: int = 9,
+            n_planes: int = 48, s_max: int = 96):
+    """The batched workload: the 64-antenna 3 km array on n_ch channels from 100
+    to 200 MHz (uv scaled by frequency, one grid per channel: 1024^2, 2048^2 or
+    4096^2 by channel band) plus n_facets facets (1024^2, 2048^2, 4096^2) of the
+    150 MHz data; one field of view for all (pixel size scales with the grid),
+    so all members share one set of n_planes w-planes (S 8..s_max) over the
+    global w range.  Default: 73 grids x 435,456 vis = 31.8 M visibilities.
+    Returns (members, scale, supports, w_planes, w_low, w_high)."""
+    from .gcf import plane_supports
+
+    rng = np.random.default_rng(SEED0 + 3 if seed is None else seed)
+    ant = antennas_disk(rng, 64, 3000.0)
+    uvw_m = uvw_tracks(ant, n_t).reshape(-1, 3)
+    freqs = np.linspace(100e6, 200e6, n_ch)
+    sizes = [1024 if k < n_ch // 3 else 2048 if k < 2 * n_ch // 3 else 4096 for k in range(n_ch)]
+    l, m, flux = sky(rng)
+    uvws, grids = [], []
+    for f, G in zip(freqs, sizes):
+        uvws.append(uvw_m * (f / C_LIGHT))
+        grids.append(G)
+    f150 = uvw_m * (150e6 / C_LIGHT)
+    for k in range(n_facets):
+        uvws.append(f150)
+        grids.append([1024, 2048, 4096][k % 3])
+    # one FoV: every member's max |uv| fits 90 % of its half-grid
+    scale = min(0.9 * (G / 2) / float(np.sqrt(u[:, 0] ** 2 + u[:, 1] ** 2).max())
+                for u, G in zip(uvws, grids))
+    wmin = min(0.0, min(float(u[:, 2].min()) for u in uvws))
+    wmax0 = max(0.0, max(float(u[:, 2].max()) for u in uvws))
+    w_high = wmax0 + (wmax0 - wmin) * 1e-4
+    supports, centres = plane_supports(wmin, w_high, n_planes, 8, s_max)
+    members = []
+    for k, (u, G) in enumerate(zip(uvws, grids)):
+        vis = predict(u, l, m, flux, rng)
+        members.append(Observation(f"c3.{k}", np.ascontiguousarray(u), vis, G, scale, n_planes,
+                                   supports, centres, wmin, w_high, int(supports.max()),
+                                   u.shape[0] // n_t, n_t, 1))
+    return members, scale, supports, centres, wmin, w_high
+
+
 def config(name: str, seed: int | None = None, n_t: int | None = None) -> Observation:
     """Build a workload by name ('c1', 'c2', 'c4', 'c5'; 'small' for tests).
     n_t overrides the number of time samples (for reduced test sizes)."""
