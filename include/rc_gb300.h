@@ -195,6 +195,38 @@ int gb_gcf_generate(int32_t n_planes, const double *w_planes, const int32_t *sup
                     const int64_t *gcf_offsets, int32_t max_support, double t2,
                     const double *d_taper, double *d_gcf64, float *d_gcf32, void *stream);
 
+/* Hogbom CLEAN minor loop on the GPU (engine form, FP32), replacing the
+ * reference's kern_hogbom_* minor cycles (MS6/kernel/cpu/gridding/hogbom.cpp)
+ * and the MS4 GPU peak-find / PSF-subtract kernels (MS4/kernel/gpu/hogbom/
+ * hogbom.cu:31-53).  n_iter iterations of: peak = residual pixel of largest
+ * |value| (lowest row-major index on ties); stop when |peak| < threshold;
+ * residual -= (gain * peak / psf[ppy][ppx]) * psf shifted so that its peak
+ * (psf_peak_x, psf_peak_y) lands on the residual peak (zero outside the PSF);
+ * model[peak] += gain * peak.  Images are row-major nx * ny floats; the PSF
+ * pnx * pny.  d_work: gb_hogbom_work_bytes() bytes of device scratch.  One
+ * launch per iteration, no synchronisation: the sequence can be captured in
+ * a CUDA graph.  gb_hogbom_iterations reads back how many iterations
+ * subtracted a component (synchronises). */
+int gb_hogbom_work_bytes(int32_t nx, int32_t ny, int64_t *bytes);
+int gb_hogbom_f32(float *d_residual, int32_t nx, int32_t ny, const float *d_psf, int32_t pnx,
+                  int32_t pny, int32_t psf_peak_x, int32_t psf_peak_y, float gain,
+                  float threshold, int32_t n_iter, float *d_model, void *d_work,
+                  int64_t work_bytes, void *stream);
+int gb_hogbom_iterations(const void *d_work, int32_t *iterations, void *stream);
+
+/* The reference's CLEAN kernels (host FP64 images, synchronous), with the
+ * reference's own rules: 12 cycles, the "PSF peak" taken as the argmax of
+ * |res| over the PSF's extent, the absolute peak value used for subtraction
+ * and model, clamped PSF shift; kern_hogbom_model accumulates into `model`,
+ * kern_hogbom_residual writes the residual of the cycle that first fell under
+ * the threshold (or of the last cycle).
+ * replace MS6/kernel/cpu/gridding/hogbom.cpp:128-129, bound at
+ * MS6/programs/Kernel/Cleaning.hs:22-44 */
+int kern_hogbom_model(double gain, double threshold, buffer_t *psf, buffer_t *res,
+                      buffer_t *model);
+int kern_hogbom_residual(double gain, double threshold, buffer_t *psf, buffer_t *res,
+                         buffer_t *residual);
+
 /* Batched FP32 gridding / degridding: up to GB_MAX_BATCH grids (channels,
  * facets, data sets; any sizes and w-plane sets) in ONE persistent launch fed
  * by one device work queue, longest work first.  The reference runs such units

@@ -279,3 +279,69 @@ def ms4_degrid(scale, uvw_bl, grid_ms6, gcf_ms6):
                                  gss.ctypes.data)
     del keep
     return out
+
+
+# ---------------------------------------------------------------- Hogbom CLEAN
+def hogbom_f32(res, psf, ppx, ppy, gain, threshold, n_iter):
+    """The engine's CLEAN in numpy float32 (what gb_hogbom_f32 must reproduce
+    bit for bit): peak = largest |res| (first in row-major order), stop under
+    threshold, res -= (gain*peak/psf[ppy,ppx]) * shifted psf, model[peak] +=
+    gain*peak.  Returns (residual, model, iterations)."""
+    res = np.array(res, np.float32, copy=True)
+    psf = np.asarray(psf, np.float32)
+    model = np.zeros_like(res)
+    ny, nx = res.shape
+    pny, pnx = psf.shape
+    g = np.float32(gain)
+    th = np.float32(threshold)
+    pp = psf[ppy, ppx]
+    done = 0
+    for _ in range(n_iter):
+        a = np.abs(res)
+        idx = int(np.argmax(a))
+        if a.flat[idx] < th or pp == 0:
+            break
+        val = res.flat[idx]
+        py, px = divmod(idx, nx)
+        s = np.float32(np.float32(g * val) / pp)
+        dx, dy = px - ppx, py - ppy
+        x0, x1 = max(0, dx), min(nx, dx + pnx)
+        y0, y1 = max(0, dy), min(ny, dy + pny)
+        if x0 < x1 and y0 < y1:
+            res[y0:y1, x0:x1] = res[y0:y1, x0:x1] - s * psf[y0 - dy:y1 - dy, x0 - dx:x1 - dx]
+        model.flat[idx] = np.float32(model.flat[idx] + np.float32(g * val))
+        done += 1
+    return res, model, done
+
+
+def hogbom_reference(gain, threshold, psf, res, model=None, cycles=12):
+    """MS6/kernel/cpu/gridding/hogbom.cpp:30-109 restated (FP64): the "PSF
+    peak" is argmax |res| over the PSF's extent (:58), peak values are
+    absolute (:85-90), the shift is clamped (:99-100), the model gets
+    gain*|peak| (:108); the residual is the one of the cycle at which the
+    threshold is first crossed, else the last (:68-74).  Returns (model, residual)."""
+    res = np.array(res, np.float64, copy=True)
+    psf = np.asarray(psf, np.float64)
+    model = np.zeros_like(res) if model is None else np.array(model, np.float64, copy=True)
+    ny, nx = res.shape
+    pny, pnx = psf.shape
+    sub = np.abs(res[:min(pny, ny), :min(pnx, nx)])
+    ppy, ppx = divmod(int(np.argmax(sub)), sub.shape[1])
+    pval = sub[ppy, ppx]
+    yy, xx = np.mgrid[0:ny, 0:nx]
+    for _ in range(cycles):
+        a = np.abs(res)
+        idx = int(np.argmax(a))
+        val = a.flat[idx]
+        if val < threshold:
+            break
+        py, px = divmod(idx, nx)
+        dx = min(max(px - ppx, -pnx), nx)
+        dy = min(max(py - ppy, -pny), ny)
+        qx, qy = xx - dx, yy - dy
+        inside = (qx >= 0) & (qx < pnx) & (qy >= 0) & (qy < pny)
+        shifted = np.zeros_like(res)
+        shifted[inside] = psf[qy[inside], qx[inside]]
+        res = res - (gain * val / pval) * shifted
+        model[min(max(py, 0), ny - 1), min(max(px, 0), nx - 1)] += gain * val
+    return model, res

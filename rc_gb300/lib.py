@@ -109,6 +109,13 @@ SIGNATURES = {
                                   C.POINTER(C.c_int64), C.c_int32, C.c_double, _VP, _VP, _VP,
                                   _VP]),
     "gb_grid_zero_f32": (C.c_int, [_VP, C.c_int64, _VP]),
+    "gb_hogbom_work_bytes": (C.c_int, [C.c_int32, C.c_int32, C.POINTER(C.c_int64)]),
+    "gb_hogbom_f32": (C.c_int, [_VP, C.c_int32, C.c_int32, _VP, C.c_int32, C.c_int32, C.c_int32,
+                                C.c_int32, C.c_float, C.c_float, C.c_int32, _VP, _VP, C.c_int64,
+                                _VP]),
+    "gb_hogbom_iterations": (C.c_int, [_VP, C.POINTER(C.c_int32), _VP]),
+    "kern_hogbom_model": (C.c_int, [C.c_double, C.c_double, _BP, _BP, _BP]),
+    "kern_hogbom_residual": (C.c_int, [C.c_double, C.c_double, _BP, _BP, _BP]),
     "gb_batch_create": (C.c_int, [C.c_int32, C.POINTER(BatchMember), _VP, C.POINTER(_VP)]),
     "gb_batch_destroy": (C.c_int, [_VP]),
     "gb_batch_stats": (C.c_int, [_VP, C.POINTER(C.c_int64)]),
