@@ -111,3 +111,35 @@ def generate(w_planes, supports, max_support, t2, taper=None, want64=True, want3
                                  g32.data_ptr() if g32 is not None else None, st),
                "gb_gcf_generate")
     return g64, g32, offs
+
+
+def grid_correction(gcf_plane, n, offsets="generator", over=OVER):
+    """Image-domain grid-correction function of an oversampled GCF plane.
+
+    gcf_plane: one plane's GCF, [64][S][S] complex (phase ou + 8 ov, MS6
+    layout), normally a w = 0 kernel.  The kernel is taken as separable: the
+    1-D kernel of phase ou is the column sum of phase (ou, 0).  `offsets` says
+    where tap sx of phase ou was sampled: "generator" d = sx - S/2 + ou/8 cells
+    (the w-kernel generator, GCF.cpp:39-47) or "centred" d = sx - S/2 - ou/8
+    (a kernel centred on the visibility under the MS6 index math, as
+    pswf_uv_gcf builds it).  Returns c(j) = Re sum_d K(d) exp(2 pi i d
+    (j - n/2) / n) / over for the n image pixels: the transform of the kernel
+    the samples come from, 1 at the centre if the kernel sums to 1."""
+    g = np.asarray(gcf_plane).reshape(over * over, -1)
+    S = int(round(np.sqrt(g.shape[1])))
+    g = g.reshape(over, over, S, S)  # [ov][ou][sy][sx]
+    k = g[0].sum(axis=1)  # [ou][sx]: sum over sy of phase (ou, ov=0)
+    sign = {"generator": 1.0, "centred": -1.0}[offsets]
+    d = (np.arange(S)[None, :] - S // 2 + sign * np.arange(over)[:, None] / over).ravel()
+    kv = k.ravel()
+    l = (np.arange(n) - n // 2) / n
+    return np.real(np.exp(2j * np.pi * np.outer(l, d)) @ kv) / over
+
+
+def w0_correction(max_support, t2, taper, n, support=8, device="cuda"):
+    """Grid correction of a w-projection GCF set: the image response of its
+    w = 0 kernel (same generator, field of view and taper), generated on the
+    GPU and transformed by grid_correction()."""
+    _, g32, _ = generate([0.0], [support], max_support, t2, taper=taper, want64=False,
+                         device=device)
+    return grid_correction(g32.cpu().numpy(), n)

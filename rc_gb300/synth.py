@@ -17,7 +17,8 @@ Workloads (sizes as the benchmark configurations state them):
   c4  c1's array, 2,064,384 vis (2016 bl x 1024 t), 2048^2 grid,
       16 w-planes, S 8..64 (the least-squares imaging layout).
   c5  512 stations log-radial to 40 km, 130,816 bl x 64 t x 4 ch,
-      8192^2 grid, 64 w-planes, S 8..128.
+      8192^2 grid, 64 w-planes, S 8..128; its sources lie within +-0.2 of the
+      field of view (the field is only +-0.046 rad wide).
 """
 from __future__ import annotations
 
@@ -130,18 +131,19 @@ def sky_image(n, rng, n_blobs=20, sigma=(1.0, 5.0), flux=(0.1, 10.0), margin=0.2
     return img.astype(np.float32)
 
 
-def _finish(name, rng, uvw_m, freqs, grid_size, n_planes, s_min, s_max):
-    """metres -> wavelengths per channel, sky, scale, w-planes."""
+def _finish(name, rng, uvw_m, freqs, grid_size, n_planes, s_min, s_max, lm_field=None):
+    """metres -> wavelengths per channel, sky, scale, w-planes.  lm_field: if
+    given, sources lie within +-lm_field * (field of view) instead of +-0.05 rad."""
     from .gcf import plane_supports
 
     n_bl, n_t, _ = uvw_m.shape
     per_ch = [uvw_m.reshape(-1, 3) * (f / C_LIGHT) for f in freqs]
     # channel-minor ordering within each (baseline, time): [bl][t][ch]
     uvw = np.stack(per_ch, 1).reshape(-1, 3) if len(freqs) > 1 else per_ch[0]
-    l, m, flux = sky(rng)
-    vis = predict(uvw, l, m, flux, rng)
     maxuv = float(np.sqrt(uvw[:, 0] ** 2 + uvw[:, 1] ** 2).max())
     scale = 0.9 * (grid_size / 2) / maxuv
+    l, m, flux = sky(rng, lm_max=0.05 if lm_field is None else lm_field * scale)
+    vis = predict(uvw, l, m, flux, rng)
     if n_planes > 1:
         w = uvw[:, 2]
         low = min(0.0, float(w.min()))
@@ -217,7 +219,8 @@ def config(name: str, seed: int | None = None, n_t: int | None = None) -> Observ
         ant = antennas_logradial(rng, 512, 1000.0, 40000.0)
         uvw_m = uvw_tracks(ant, n_t or 64)
         freqs = [150e6 * (1 + 0.01 * k) for k in range(4)]
-        return _finish(name, rng, uvw_m, freqs, 8192, 64, 8, 128)
+        # the 40 km array's field is +-0.046 rad: keep the sources in its inner half
+        return _finish(name, rng, uvw_m, freqs, 8192, 64, 8, 128, lm_field=0.2)
     # small: quick w-projection case for tests
     ant = antennas_logradial(rng, 24, 300.0, 3000.0)
     uvw_m = uvw_tracks(ant, n_t or 32)
