@@ -227,6 +227,29 @@ int kern_hogbom_model(double gain, double threshold, buffer_t *psf, buffer_t *re
 int kern_hogbom_residual(double gain, double threshold, buffer_t *psf, buffer_t *res,
                          buffer_t *residual);
 
+/* De-tiling and facet rotation, the steps either side of tiled / faceted
+ * gridding strategies.
+ * kern_detile: out(c,x,y) += in(c,x,y) over the overlap of the two buffers'
+ *   (min, extent) regions; replaces MS6/kernel/cpu/gridding/detile.cpp:10-39
+ *   (bound at MS6/programs/Kernel/Gridder.hs:81-85).
+ * kern_rotate: facet phase rotation vis * exp(2 pi i ((0,0,1) - R (0,0,1)) . uvw)
+ *   and, with uvproj != 0, uvw reprojection, R = xyz2uvw(out) * uvw2xyz(in),
+ *   out_lon = out_lon0 + out->min[2] * out_lon_incr (lat likewise, min[3]);
+ *   replaces MS6/kernel/cpu/gridding/rotate.cpp:11-84 (bound at
+ *   MS6/programs/Kernel/Facet.hs:25-54).
+ * gb_detile_f32 / gb_rotate_f64: the same on device buffers (complex64 grids
+ * with row pitches; 5-double visibility records). */
+int kern_detile(buffer_t *in_grid, buffer_t *out_grid);
+int kern_rotate(double in_lon, double in_lat, double out_lon0, double out_lat0,
+                double out_lon_incr, double out_lat_incr, int32_t uvproj, buffer_t *vis,
+                buffer_t *out);
+int gb_detile_f32(const float *d_tile, int64_t tile_pitch, int32_t tile_min_x,
+                  int32_t tile_min_y, int32_t tile_w, int32_t tile_h, float *d_grid,
+                  int64_t grid_pitch, int32_t grid_min_x, int32_t grid_min_y, int32_t grid_w,
+                  int32_t grid_h, void *stream);
+int gb_rotate_f64(double in_lon, double in_lat, double out_lon, double out_lat, int32_t uvproj,
+                  int64_t n, const double *d_vis5, double *d_out5, void *stream);
+
 /* Batched FP32 gridding / degridding: up to GB_MAX_BATCH grids (channels,
  * facets, data sets; any sizes and w-plane sets) in ONE persistent launch fed
  * by one device work queue, longest work first.  The reference runs such units
@@ -312,6 +335,17 @@ int gb_image_to_grid_f64(const double *d_image, const double *d_taper, int32_t n
                          double *d_grid, void *stream);
 int gb_grid_to_image_f64(const double *d_grid, const double *d_taper, int32_t n, double *d_work,
                          double *d_image, void *stream);
+
+/* GCF choice for a w-region [w0, w1] among precomputed GCFs of nominal w
+ * w_files[i]: the largest w_files[i] <= max(|w0|, |w1|) (the last of equal
+ * ones), and whether to conjugate it (w0 < -w1: a mostly negative-w region).
+ * replaces gcfGet (MS6/programs/Kernel/Config.hs:128-132) and the conjugation
+ * of gcfKernel (MS6/programs/Kernel/IO.hs:97-115).  Host logic, no GPU. */
+int gb_gcf_select(int32_t n_files, const double *w_files, double w0, double w1, int32_t *index,
+                  int32_t *conjugate);
+/* Conjugate a device GCF array in place (negate the imaginary parts). */
+int gb_gcf_conjugate_f32(float *d_gcf, int64_t n_complex, void *stream);
+int gb_gcf_conjugate_f64(double *d_gcf, int64_t n_complex, void *stream);
 
 /* Zero `n_complex` complex64 grid elements (device). */
 int gb_grid_zero_f32(float *d_grid, int64_t n_complex, void *stream);

@@ -345,3 +345,68 @@ def hogbom_reference(gain, threshold, psf, res, model=None, cycles=12):
         res = res - (gain * val / pval) * shifted
         model[min(max(py, 0), ny - 1), min(max(px, 0), nx - 1)] += gain * val
     return model, res
+
+
+# ---------------------------------------------------------------- detile / rotate
+def detile(in_grid, in_min, out_grid, out_min):
+    """MS6/kernel/cpu/gridding/detile.cpp:16-30: out += in over the overlap of
+    the two (min, extent) regions.  Grids are complex [H][W]; mins (x, y)."""
+    out = np.array(out_grid, copy=True)
+    ih, iw = in_grid.shape
+    oh, ow = out.shape
+    x0, x1 = max(in_min[0], out_min[0]), min(in_min[0] + iw, out_min[0] + ow)
+    y0, y1 = max(in_min[1], out_min[1]), min(in_min[1] + ih, out_min[1] + oh)
+    if x1 > x0 and y1 > y0:
+        out[y0 - out_min[1]:y1 - out_min[1], x0 - out_min[0]:x1 - out_min[0]] += \
+            in_grid[y0 - in_min[1]:y1 - in_min[1], x0 - in_min[0]:x1 - in_min[0]]
+    return out
+
+
+def _rx(p):
+    s, c = np.sin(p), np.cos(p)
+    return np.array([[1, 0, 0], [0, c, -s], [0, s, c]])
+
+
+def _rz(p):
+    s, c = np.sin(p), np.cos(p)
+    return np.array([[c, -s, 0], [s, c, 0], [0, 0, 1]])
+
+
+def rotate(in_lon, in_lat, out_lon, out_lat, uvproj, vis5):
+    """MS6/kernel/cpu/gridding/rotate.cpp:36-66 with utils.h:119-163: R =
+    xyz2uvw(out) uvw2xyz(in); uvw' = (R^T inv2x2(R)^T R) uvw if uvproj else
+    uvw; vis' = vis * exp(2 pi i ((0,0,1) - R (0,0,1)) . uvw)."""
+    xyz2uvw = _rx(-np.pi / 2 + out_lat) @ _rz(-np.pi / 2 - out_lon)
+    uvw2xyz = _rz(np.pi / 2 + in_lon) @ _rx(np.pi / 2 - in_lat)
+    R = xyz2uvw @ uvw2xyz
+    if uvproj:
+        det = R[0, 0] * R[1, 1] - R[0, 1] * R[1, 0]
+        inv = np.array([[R[1, 1] / det, -R[0, 1] / det, 0], [-R[1, 0] / det, R[0, 0] / det, 0],
+                        [0, 0, 1]])
+        M = R.T @ (inv.T @ R)
+    else:
+        M = np.eye(3)
+    uvw = vis5[:, :3]
+    pc = np.array([0.0, 0.0, 1.0]) - R @ np.array([0.0, 0.0, 1.0])
+    path = uvw @ pc
+    v = (vis5[:, 3] + 1j * vis5[:, 4]) * np.exp(2j * np.pi * path)
+    out = np.empty_like(vis5)
+    out[:, :3] = uvw @ M.T
+    out[:, 3], out[:, 4] = v.real, v.imag
+    return out
+
+
+# ---------------------------------------------------------------- GCF choice
+def gcf_select(w_files, w0, w1):
+    """Config.hs:128-132 (maximumBy (comparing gcfW) . filter ((<= w) . gcfW),
+    w = max |w0| |w1|; maximumBy keeps the last of equal maxima) and
+    IO.hs:110-113 (conjugate when low < -high).  Raises if nothing qualifies."""
+    w = max(abs(w0), abs(w1))
+    cand = [i for i, x in enumerate(w_files) if x <= w]
+    if not cand:
+        raise ValueError("no GCF with w <= %g" % w)
+    best = cand[0]
+    for i in cand[1:]:
+        if w_files[i] >= w_files[best]:
+            best = i
+    return best, w0 < -w1

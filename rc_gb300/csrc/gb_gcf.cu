@@ -199,3 +199,60 @@ done:
   cudaFree(sums);
   return rc;
 }
+
+// ---------------------------------------------------------------- GCF choice per w-region
+// MS6/programs/Kernel/Config.hs:128-132: the GCF file with the largest w not
+// above max(|w0|, |w1|) (maximumBy keeps the last of equal maxima); and
+// MS6/programs/Kernel/IO.hs:110-113: conjugate when the region lies mostly at
+// negative w (low < -high).
+extern "C" int gb_gcf_select(int32_t n_files, const double* w_files, double w0, double w1,
+                             int32_t* index, int32_t* conjugate) {
+  if (n_files < 1 || !w_files || !index || !conjugate) {
+    gb_set_error(GB_ERR_ARG, "gb_gcf_select: bad arguments");
+    return GB_ERR_ARG;
+  }
+  const double w = fabs(w0) > fabs(w1) ? fabs(w0) : fabs(w1);
+  int best = -1;
+  for (int i = 0; i < n_files; i++)
+    if (w_files[i] <= w && (best < 0 || w_files[i] >= w_files[best])) best = i;
+  if (best < 0) {
+    gb_set_error(GB_ERR_ARG, "gb_gcf_select: no GCF with w <= %g", w);
+    return GB_ERR_ARG;
+  }
+  *index = best;
+  *conjugate = w0 < -w1 ? 1 : 0;
+  return GB_OK;
+}
+
+namespace gb {
+template <class C>
+__global__ void k_conjugate(C* __restrict__ g, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    g[i].y = -g[i].y;
+}
+}  // namespace gb
+
+extern "C" int gb_gcf_conjugate_f32(float* d_gcf, int64_t n_complex, void* stream) {
+  if (!d_gcf || n_complex < 0) {
+    gb_set_error(GB_ERR_ARG, "gb_gcf_conjugate_f32: bad arguments");
+    return GB_ERR_ARG;
+  }
+  if (!n_complex) return GB_OK;
+  const int b = (int)std::min<int64_t>((n_complex + 255) / 256, 4096);
+  k_conjugate<float2><<<b, 256, 0, (cudaStream_t)stream>>>((float2*)d_gcf, n_complex);
+  GB_CUDA_TRY(cudaGetLastError());
+  return GB_OK;
+}
+
+extern "C" int gb_gcf_conjugate_f64(double* d_gcf, int64_t n_complex, void* stream) {
+  if (!d_gcf || n_complex < 0) {
+    gb_set_error(GB_ERR_ARG, "gb_gcf_conjugate_f64: bad arguments");
+    return GB_ERR_ARG;
+  }
+  if (!n_complex) return GB_OK;
+  const int b = (int)std::min<int64_t>((n_complex + 255) / 256, 4096);
+  k_conjugate<double2><<<b, 256, 0, (cudaStream_t)stream>>>((double2*)d_gcf, n_complex);
+  GB_CUDA_TRY(cudaGetLastError());
+  return GB_OK;
+}

@@ -143,3 +143,13 @@ def w0_correction(max_support, t2, taper, n, support=8, device="cuda"):
     _, g32, _ = generate([0.0], [support], max_support, t2, taper=taper, want64=False,
                          device=device)
     return grid_correction(g32.cpu().numpy(), n)
+
+
+def select(w_files, w0, w1):
+    """(index, conjugate) of the GCF for the w-region [w0, w1] (gb_gcf_select)."""
+    w = np.ascontiguousarray(w_files, np.float64)
+    idx, conj = C.c_int32(), C.c_int32()
+    L = _lib.load()
+    _lib.check(L.gb_gcf_select(len(w), w.ctypes.data_as(C.POINTER(C.c_double)), float(w0),
+                               float(w1), C.byref(idx), C.byref(conj)), "gb_gcf_select")
+    return idx.value, bool(conj.value)

@@ -109,12 +109,21 @@ SIGNATURES = {
                                   C.POINTER(C.c_int64), C.c_int32, C.c_double, _VP, _VP, _VP,
                                   _VP]),
     "gb_grid_zero_f32": (C.c_int, [_VP, C.c_int64, _VP]),
+    "gb_gcf_select": (C.c_int, [C.c_int32, C.POINTER(C.c_double), C.c_double, C.c_double,
+                                C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
+    "gb_gcf_conjugate_f32": (C.c_int, [_VP, C.c_int64, _VP]),
+    "gb_gcf_conjugate_f64": (C.c_int, [_VP, C.c_int64, _VP]),
     "gb_hogbom_work_bytes": (C.c_int, [C.c_int32, C.c_int32, C.POINTER(C.c_int64)]),
     "gb_hogbom_f32": (C.c_int, [_VP, C.c_int32, C.c_int32, _VP, C.c_int32, C.c_int32, C.c_int32,
                                 C.c_int32, C.c_float, C.c_float, C.c_int32, _VP, _VP, C.c_int64,
                                 _VP]),
     "gb_hogbom_iterations": (C.c_int, [_VP, C.POINTER(C.c_int32), _VP]),
     "kern_hogbom_model": (C.c_int, [C.c_double, C.c_double, _BP, _BP, _BP]),
+    "kern_detile": (C.c_int, [_BP, _BP]),
+    "kern_rotate": (C.c_int, [C.c_double] * 6 + [C.c_int32, _BP, _BP]),
+    "gb_detile_f32": (C.c_int, [_VP, C.c_int64, C.c_int32, C.c_int32, C.c_int32, C.c_int32, _VP,
+                                C.c_int64, C.c_int32, C.c_int32, C.c_int32, C.c_int32, _VP]),
+    "gb_rotate_f64": (C.c_int, [C.c_double] * 4 + [C.c_int32, C.c_int64, _VP, _VP, _VP]),
     "kern_hogbom_residual": (C.c_int, [C.c_double, C.c_double, _BP, _BP, _BP]),
     "gb_batch_create": (C.c_int, [C.c_int32, C.POINTER(BatchMember), _VP, C.POINTER(_VP)]),
     "gb_batch_destroy": (C.c_int, [_VP]),

@@ -35,3 +35,20 @@ def test_gcf_generation_rejects_bad_arguments():
         G.generate([0.0], [10], 8, 0.1)  # support > max_support
     with pytest.raises(lib.GbError):
         G.generate([0.0], [8], 9, 0.1)  # odd max_support
+
+
+def test_gcf_conjugate_on_device():
+    import ctypes as C
+
+    import torch
+
+    from rc_gb300 import lib
+
+    L = lib.load()
+    rng = np.random.default_rng(2)
+    g = rng.standard_normal(1000) + 1j * rng.standard_normal(1000)
+    for dt, fn in [(torch.complex64, L.gb_gcf_conjugate_f32), (torch.complex128,
+                                                               L.gb_gcf_conjugate_f64)]:
+        d = torch.tensor(g, dtype=dt, device="cuda")
+        lib.check(fn(d.data_ptr(), d.numel(), torch.cuda.current_stream().cuda_stream), "conj")
+        assert np.array_equal(d.cpu().numpy(), np.conj(g.astype(d.cpu().numpy().dtype)))
