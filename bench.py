@@ -688,6 +688,206 @@ def our_arm_major_cycle(args):
     return 0
 
 
+# ---------------------------------------------------------------- OSKAR ingest
+OSKAR_METRIC = "Mvis/s OSKAR .vis ingest (read, CRC-32C check, reshuffle to [bl][t][ch], u,v,w to wavelengths)"
+
+
+def _oskar_file(ob, path, writer):
+    """The config-2 observation as an OSKAR 2.6 file (blocks of 8 times)."""
+    t0 = time.perf_counter()
+    if writer == "ours":
+        from rc_gb300 import synth
+        size = synth.write_oskar_vis(path, ob, max_times_per_block=8)
+    else:  # the reference arm runs none of the engine's code
+        from oracle import oskar as K
+        B, T = ob.n_bl, ob.n_t
+        S = int(round((1 + (1 + 8 * B) ** 0.5) / 2))
+        vis = ob.vis.reshape(B, T).T
+        amps = np.zeros((T, 1, B, 4), np.complex128)
+        amps[:, 0, :, 0] = vis
+        amps[:, 0, :, 3] = vis
+        m = (ob.uvw * (299792458.0 / 150e6)).reshape(B, T, 3).transpose(2, 1, 0)
+        lay = K.layout(S, T, 1, 8, freq_start_hz=150e6, freq_inc_hz=0.0)
+        assert K.write(path, lay, amps, m[0], m[1], m[2]) == 0
+        size = os.path.getsize(path)
+    return size, time.perf_counter() - t0
+
+
+def our_arm_oskar(args):
+    """OSKAR ingest: the config-2 observation (256 stations, 32,640 baselines x
+    128 times x 1 channel = 4,177,920 points) stored as an OSKAR 2.6 .vis file
+    in blocks of 8 times (367 MB), in the page cache.  One step = open + index +
+    read every block: small tags on the host; payloads by parallel pread into
+    pinned slots and copies to HBM; CRC-32C of every payload and the reshuffle
+    [t][c][b] -> [b][t][c] with the wavelength scaling and extrema on the GPU.
+    value: outputs left in HBM (gb_oskar_read_device); e2e: the reference ABI
+    (mkFromFile + readAndReshuffle) into host arrays; cpu_baseline: the C
+    restatement of the reference reader (single thread, as the reference)."""
+    import ctypes as C
+    import tempfile
+
+    import torch
+
+    from rc_gb300 import lib as Lm
+    from rc_gb300 import synth
+
+    L = Lm.load()
+    dev = torch.device("cuda", 0)
+    ob = synth.config("c2")
+    tmpdir = tempfile.mkdtemp(prefix="rc_oskar_")
+    path = os.path.join(tmpdir, "c2.vis")
+    fsize, write_s = _oskar_file(ob, path, "ours")
+    pb = path.encode()
+    vd = Lm.VisData()
+    Lm.check(L.mkFromFile(C.byref(vd), pb), "mkFromFile")
+    P, B = vd.num_points, vd.num_baselines
+    L.freeBinHandler(C.byref(vd))
+    d_amps = torch.empty((P, 4), dtype=torch.complex128, device=dev)
+    d_uvw = torch.empty((P, 3), dtype=torch.float64, device=dev)
+    mx = Lm.Metrix()
+    blw = (Lm.WMaxMin * B)()
+    stream = torch.cuda.current_stream().cuda_stream
+    tm = (C.c_double * 4)()
+
+    def dev_step():
+        v = Lm.VisData()
+        Lm.check(L.mkFromFile(C.byref(v), pb), "mkFromFile")
+        try:
+            Lm.check(L.gb_oskar_read_device(C.byref(v), d_amps.data_ptr(), d_uvw.data_ptr(),
+                                            C.byref(mx), blw, stream), "gb_oskar_read_device")
+        finally:
+            L.freeBinHandler(C.byref(v))
+        L.gb_oskar_last_timings(tm)
+        return list(tm)
+
+    for _ in range(args.warmup):
+        dev_step()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    per = []
+    with ClockSampler(0) as clk:
+        e0.record()
+        for _ in range(args.steps):
+            per.append(dev_step())
+        e1.record()
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    per = np.array(per)
+    stage_ms, crc_ms, resh_ms = (float(np.median(per[:, k])) for k in range(3))
+    # e2e through the reference ABI with host arrays (what the Haskell reader calls)
+    amps_h = np.empty((P, 4), np.complex128)
+    uvw_h = np.empty((P, 3), np.float64)
+    mx_h = Lm.Metrix()
+    blw_h = (Lm.WMaxMin * B)()
+
+    def host_step():
+        v = Lm.VisData()
+        Lm.check(L.mkFromFile(C.byref(v), pb), "mkFromFile")
+        try:
+            Lm.check(L.readAndReshuffle(C.byref(v), amps_h.ctypes.data, uvw_h.ctypes.data,
+                                        C.byref(mx_h), blw_h), "readAndReshuffle")
+        finally:
+            L.freeBinHandler(C.byref(v))
+
+    host_step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        host_step()
+    e2e_ms = 1e3 * (time.perf_counter() - t0) / args.steps
+    same_dev = bool(np.array_equal(d_amps.cpu().numpy().view(np.uint8), amps_h.view(np.uint8))
+                    and np.array_equal(d_uvw.cpu().numpy().view(np.uint8), uvw_h.view(np.uint8)))
+    cpu = None
+    parity = None
+    if not args.no_cpu:
+        from oracle import oskar as K
+        reps = max(1, min(3, args.steps))
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            st, h, a_o, uvw_o, mx_o, bl_o = K.read(path)
+        cpu_s = (time.perf_counter() - t0) / reps
+        parity = bool(st == 0 and np.array_equal(a_o.view(np.uint8), amps_h.view(np.uint8)) and
+                      np.array_equal(uvw_o.view(np.uint8), uvw_h.view(np.uint8)))
+        cpu = {"value": round(P / cpu_s / 1e6, 3), "unit": "Mvis/s", "cores": 1, "kind": "port",
+               "sample": f"the whole {fsize / 1e6:.0f} MB file ({P} points), C restatement of "
+                         "mkFromFile + readAndReshuffle (fread, CRC-32C slicing-by-8, reshuffle)",
+               "ms": round(1e3 * cpu_s, 1)}
+    os.remove(path)
+    os.rmdir(tmpdir)
+    peak, peak_kind = measured_peaks()
+    payload = P * 88  # per point: 64 B of 4-pol amplitudes + 24 B of u,v,w (one channel)
+    dom = "k_crc32c" if crc_ms >= resh_ms else "k_oskar_reshuffle"
+    dom_bytes = payload if dom == "k_crc32c" else 2 * payload
+    dom_ms = max(crc_ms, resh_ms)
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tpath):
+        traffic = json.load(open(tpath)).get("oskar", {}).get(dom)
+    line = {
+        "metric": OSKAR_METRIC, "value": round(P / (ms * 1e-3) / 1e6, 3), "unit": "Mvis/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded) config-2 observation written as an OSKAR 2.6 file",
+        "config": {"workload": f"OSKAR .vis of c2: {B} baselines x {vd.num_times} times x 1 "
+                               f"channel = {P} points, blocks of 8 times, {fsize} bytes, file "
+                               "in the page cache; inputs larger than L2",
+                   "file_write_s": round(write_s, 1), "outputs_bitexact_device_vs_host": same_dev,
+                   "parity_vs_oracle_bitexact": parity},
+        "roofline": {"bound": "hbm", "kernel": dom,
+                     "achieved": round(dom_bytes / (dom_ms * 1e-3) / 1e9, 1), "peak": peak,
+                     "unit": "GB/s", "frac": round(dom_bytes / (dom_ms * 1e-3) / 1e9 / peak, 4),
+                     "peak_kind": peak_kind, "traffic": traffic,
+                     "algorithmic_bytes_per_launch": int(dom_bytes)},
+        "kernels_ms": {"host_staging_ms": round(stage_ms, 3), "k_crc32c": round(crc_ms, 4),
+                       "k_oskar_reshuffle": round(resh_ms, 4)},
+        "e2e": {"value": round(P / (e2e_ms * 1e-3) / 1e6, 3), "unit": "Mvis/s",
+                "ms_per_step": round(e2e_ms, 2), "h2d_bytes_per_step": int(payload),
+                "d2h_bytes_per_step": int(P * 88)},
+        "cpu_baseline": cpu, "gpu_launches": 3 * args.steps, "clocks": clk.summary(),
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def reference_arm_oskar(args):
+    """--impl reference --config oskar: the reference reader's semantics (its C
+    restatement, single thread as the reference) on the same file."""
+    import tempfile
+
+    from oracle import oskar as K
+    from rc_gb300 import synth
+
+    if int(os.environ.get("RANK", "0")) != 0:
+        return 0
+    ob = synth.config("c2")
+    tmpdir = tempfile.mkdtemp(prefix="rc_oskar_ref_")
+    path = os.path.join(tmpdir, "c2.vis")
+    fsize, _ = _oskar_file(ob, path, "reference")
+    for _ in range(min(args.warmup, 1)):
+        K.read(path)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        st, h, *_ = K.read(path)
+    dt = (time.perf_counter() - t0) / args.steps
+    os.remove(path)
+    os.rmdir(tmpdir)
+    P = h.num_points
+    val = P / dt / 1e6
+    line = {
+        "metric": OSKAR_METRIC, "impl": "reference", "value": round(val, 3), "unit": "Mvis/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(1e3 * dt, 2), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+        "config": {"workload": f"OSKAR .vis of c2: {P} points, {fsize} bytes, page cache",
+                   "status": st},
+        "cpu_baseline": {"value": round(val, 3), "unit": "Mvis/s", "cores": 1, "kind": "port",
+                         "sample": "whole file, C restatement of mkFromFile + readAndReshuffle"},
+        "e2e": {"value": round(val, 3), "unit": "Mvis/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -710,7 +910,9 @@ def main(argv=None):
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
     if args.impl == "reference":
-        return reference_arm(args)
+        return reference_arm_oskar(args) if args.config == "oskar" else reference_arm(args)
+    if args.config == "oskar":
+        return our_arm_oskar(args)
     if args.config == "c3":
         return our_arm_batch(args)
     if args.config == "c5":

@@ -1,4 +1,5 @@
-"""ctypes binding of librc_gb300.so (the C ABI declared in include/rc_gb300.h).
+"""ctypes binding of librc_gb300.so (the C ABI declared in include/rc_gb300.h
+and include/rc_oskar.h).
 
 The library is the only compute path: if it is missing this module raises at
 load time; there is no Python or CPU fallback.
@@ -81,6 +82,34 @@ class BatchMember(C.Structure):
 
 MAX_BATCH = 96
 
+
+class VisData(C.Structure):
+    """MS6/kernel/oskar/OskarBinReader.h:34-52 (`h` is the open file)."""
+    _fields_ = [("h", C.c_void_p), ("num_baselines", C.c_int), ("num_channels", C.c_int),
+                ("num_stations", C.c_int), ("num_times", C.c_int),
+                ("num_times_baselines", C.c_int), ("num_points", C.c_int),
+                ("phase_centre", C.c_double * 2), ("telescope_centre", C.c_double * 3),
+                ("freq_start_inc", C.c_double * 2), ("time_start_inc", C.c_double * 2),
+                ("channel_bandwidth_hz", C.c_double), ("time_average_sec", C.c_double)]
+
+
+class Metrix(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("maxu", "maxv", "maxw", "minu", "minv", "minw")]
+
+
+class WMaxMin(C.Structure):
+    _fields_ = [("maxw", C.c_double), ("minw", C.c_double)]
+
+
+OSKAR_READ_FAIL = -102
+OSKAR_FILE_INVALID = -106
+OSKAR_FORMAT_BAD = -107
+OSKAR_MEMORY_NOT_ALLOCATED = -114
+OSKAR_TAG_NOT_FOUND = -115
+OSKAR_CRC_FAIL = -118
+OSKAR_NOT_DOUBLE = 0xDEADBEEF - (1 << 32)
+OSKAR_REFERENCE_UVW_INDEX = 1
+
 # every exported symbol of include/rc_gb300.h: name -> (restype, argtypes)
 _VP = C.c_void_p
 _BP = C.POINTER(BufferT)
@@ -140,6 +169,20 @@ SIGNATURES = {
     "gb_grid_to_image_f64": (C.c_int, [_VP, _VP, C.c_int32, _VP, _VP, _VP]),
     "gb_grid_f32_noalloc": (C.c_int, [C.POINTER(Geometry), C.c_int64, _VP, C.c_int64, _VP, _VP,
                                       _VP, _VP, _VP]),
+    # include/rc_oskar.h
+    "mkFromFile": (C.c_int, [C.POINTER(VisData), C.c_char_p]),
+    "freeBinHandler": (None, [C.POINTER(VisData)]),
+    "readAndReshuffle": (C.c_int, [C.POINTER(VisData), _VP, _VP, C.POINTER(Metrix),
+                                   C.POINTER(WMaxMin)]),
+    "_aligned_malloc": (_VP, [C.c_size_t, C.c_size_t]),
+    "gb_oskar_read_device": (C.c_int, [C.POINTER(VisData), _VP, _VP, C.POINTER(Metrix),
+                                       C.POINTER(WMaxMin), _VP]),
+    "gb_oskar_records": (C.c_int, [C.POINTER(VisData), _VP, _VP, C.c_int32, C.c_int32, C.c_int64,
+                                   C.c_int64, C.c_int32, _VP, _VP]),
+    "gb_oskar_extract": (C.c_int, [C.POINTER(VisData), _VP, _VP, C.c_int32, C.c_int32, _VP, _VP,
+                                   C.c_int32, _VP]),
+    "gb_crc32c_device": (C.c_int, [_VP, C.c_int64, C.c_uint32, C.POINTER(C.c_uint32), _VP]),
+    "gb_oskar_last_timings": (C.c_int, [C.POINTER(C.c_double)]),
 }
 
 _lib = None

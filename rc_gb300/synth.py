@@ -225,3 +225,75 @@ def config(name: str, seed: int | None = None, n_t: int | None = None) -> Observ
     ant = antennas_logradial(rng, 24, 300.0, 3000.0)
     uvw_m = uvw_tracks(ant, n_t or 32)
     return _finish(name, rng, uvw_m, [150e6], 512, 8, 8, 32)
+
+
+def write_oskar_vis(path, ob: Observation, max_times_per_block: int = 8,
+                    freq_hz: float = 150e6) -> int:
+    """Store a single-channel observation as an OSKAR 2.6 visibility file, the
+    layout MS6/kernel/oskar/OskarBinReader.cpp reads (header tags in group 11,
+    blocks of max_times_per_block times in group 12, tag numbers of
+    OskarBinReader.cpp:67-100): cross-correlations [time][channel][baseline]
+    x (XX, XY, YX, YY) with XX = YY = vis and XY = YX = 0, baseline u,v,w in
+    metres (wavelengths x c / f) [time][baseline].  Every chunk carries its
+    CRC-32C, computed on the GPU.  Returns the file size in bytes."""
+    import torch
+
+    from .oskar import crc32c
+
+    assert ob.n_ch == 1, "one channel per file"
+    B, T, M = ob.n_bl, ob.n_t, int(max_times_per_block)
+    S = int(round((1 + math.sqrt(1 + 8 * B)) / 2))
+    assert S * (S - 1) // 2 == B, "baselines must be all pairs of some station count"
+    metres = (ob.uvw * (C_LIGHT / freq_hz)).reshape(B, T, 3)
+    vis = ob.vis.reshape(B, T)
+    ntpb = 7
+
+    def crc(b: bytes, code=0xFFFFFFFF):
+        if not b:
+            return code
+        t = torch.frombuffer(bytearray(b), dtype=torch.uint8).to("cuda")
+        return crc32c(t, code)
+
+    def chunk(ty, group, tag, user, payload: bytes):
+        es = {0x01: 1, 0x02: 4, 0x08: 8, 0x68: 64}[ty]
+        hdr = (b"T\x42G" + bytes([es, 0x40, ty, group, tag]) +
+               int(user).to_bytes(4, "little", signed=True) +
+               (len(payload) + 4).to_bytes(8, "little"))
+        code = crc(payload, crc(hdr))
+        return hdr + payload + int(code).to_bytes(4, "little")
+
+    i4 = lambda *x: np.array(x, np.int32).tobytes()  # noqa: E731
+    f8 = lambda *x: np.array(x, np.float64).tobytes()  # noqa: E731
+    size = 0
+    with open(path, "wb") as f:
+        parts = [b"OSKARBIN\0\x02" + bytes(54),
+                 chunk(0x01, 11, 1, 0, b"synthetic.tm\0"), chunk(0x02, 11, 2, 0, i4(ntpb)),
+                 chunk(0x02, 11, 3, 0, i4(0)), chunk(0x02, 11, 4, 0, i4(0x68)),
+                 chunk(0x02, 11, 5, 0, i4(M)), chunk(0x02, 11, 6, 0, i4(T)),
+                 chunk(0x02, 11, 7, 0, i4(1)), chunk(0x02, 11, 8, 0, i4(S)),
+                 chunk(0x08, 11, 9, 0, f8(freq_hz)), chunk(0x08, 11, 10, 0, f8(0.0)),
+                 chunk(0x08, 11, 11, 0, f8(1e6)), chunk(0x08, 11, 12, 0, f8(57000.0)),
+                 chunk(0x08, 11, 13, 0, f8(10.0)), chunk(0x08, 11, 14, 0, f8(10.0)),
+                 chunk(0x08, 11, 15, 0, f8(0.0, -45.0)),
+                 chunk(0x08, 11, 16, 0, f8(21.44, -30.0, 0.0))]
+        parts += [chunk(0x08, 11, 17 + k, 0, np.zeros(S).tobytes()) for k in range(3)]
+        for p in parts:
+            f.write(p)
+            size += len(p)
+        for blk in range((T + M - 1) // M):
+            t0 = blk * M
+            nt = min(M, T - t0)
+            amps = np.zeros((nt, 1, B, 4), np.complex128)
+            amps[:, 0, :, 0] = vis[:, t0:t0 + nt].T
+            amps[:, 0, :, 3] = vis[:, t0:t0 + nt].T
+            m = metres[:, t0:t0 + nt, :].transpose(2, 1, 0)  # [uvw][t][b]
+            for p in (chunk(0x02, 12, 1, blk, i4(t0, 0, nt, 1, B, S)),
+                      chunk(0x08, 12, 2, blk, f8(freq_hz, 0.0)),
+                      chunk(0x08, 12, 3, blk, f8(57000.0 + t0 * 10.0 / 86400.0, 10.0 / 86400.0)),
+                      chunk(0x68, 12, 5, blk, amps.tobytes()),
+                      chunk(0x08, 12, 6, blk, np.ascontiguousarray(m[0]).tobytes()),
+                      chunk(0x08, 12, 7, blk, np.ascontiguousarray(m[1]).tobytes()),
+                      chunk(0x08, 12, 8, blk, np.ascontiguousarray(m[2]).tobytes())):
+                f.write(p)
+                size += len(p)
+    return size

@@ -1,7 +1,8 @@
 """The C ABI library builds, loads, and exports every entry point that
-include/rc_gb300.h declares; buffer_t has the reference's byte layout.  No
-compute calls (these run without a GPU)."""
+include/*.h declares; buffer_t and the OSKAR reader's structs have the
+reference's byte layouts.  No compute calls (these run without a GPU)."""
 import ctypes as C
+import glob
 import os
 import re
 import subprocess
@@ -12,20 +13,42 @@ from rc_gb300 import lib
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 HEADER = os.path.join(ROOT, "include", "rc_gb300.h")
+HEADERS = sorted(glob.glob(os.path.join(ROOT, "include", "*.h")))
 
 
 def declared_functions():
-    src = open(HEADER).read()
-    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
-    names = re.findall(r"^\s*(?:const\s+)?\w+\s*\**\s*(\w+)\s*\(", src, flags=re.M)
-    return sorted(set(n for n in names if n not in ("if", "sizeof")))
+    names = set()
+    for h in HEADERS:
+        src = re.sub(r"/\*.*?\*/", "", open(h).read(), flags=re.S)
+        names |= set(re.findall(r"^\s*(?:const\s+)?\w+\s*\**\s*(\w+)\s*\(", src, flags=re.M))
+    return sorted(n for n in names if n not in ("if", "sizeof"))
 
 
 def test_header_declares_the_reference_slots():
     names = declared_functions()
     for ref in ["kern_scatter_gpu1", "kern_degrid_gpu1", "nvGridder", "kern_scatter",
-                "kern_degrid", "kern_init", "kern_psf_vis"]:
+                "kern_degrid", "kern_init", "kern_psf_vis", "mkFromFile", "freeBinHandler",
+                "readAndReshuffle", "_aligned_malloc"]:
         assert ref in names
+
+
+def test_oskar_struct_layouts_match_the_reference():
+    # MS6/kernel/oskar/OskarBinReader.h:34-72 on an LP64 host; the Haskell side
+    # reads num_baselines .. num_points at these offsets (OskarBinReaderFFI.hsc:56-60)
+    V = lib.VisData
+    assert C.sizeof(V) == 8 + 6 * 4 + 11 * 8
+    assert [getattr(V, f).offset for f in ("num_baselines", "num_channels", "num_stations",
+                                           "num_times", "num_times_baselines",
+                                           "num_points")] == [8, 12, 16, 20, 24, 28]
+    assert V.phase_centre.offset == 32 and V.time_average_sec.offset == 112
+    assert C.sizeof(lib.Metrix) == 48 and C.sizeof(lib.WMaxMin) == 16
+
+
+def test_aligned_malloc_without_gpu():
+    L = lib.load()
+    p = L._aligned_malloc(1000, 64)
+    assert p and p % 64 == 0
+    C.CDLL(None).free(C.c_void_p(p))
 
 
 def test_library_exports_every_declared_symbol():
