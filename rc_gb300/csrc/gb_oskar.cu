@@ -400,6 +400,20 @@ __device__ __forceinline__ unsigned long long order_key(double x) {
   return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
 }
 
+// Extrema are kept as order keys and compared as 64-bit integers: this part's
+// FP64 pipe is narrow, and a NaN (which never replaces a value in the
+// reference's std::max / std::min) is recognised from its bits and mapped to
+// the neutral key.
+__device__ __forceinline__ bool is_nan_bits(double x) {
+  return ((unsigned long long)__double_as_longlong(x) << 1) > 0xFFE0000000000000ull;
+}
+__device__ __forceinline__ unsigned long long key_for_max(double x) {
+  return is_nan_bits(x) ? 0ull : order_key(x);
+}
+__device__ __forceinline__ unsigned long long key_for_min(double x) {
+  return is_nan_bits(x) ? ~0ull : order_key(x);
+}
+
 double key_value(unsigned long long k) {
   const unsigned long long b = (k >> 63) ? (k & 0x7FFFFFFFFFFFFFFFull) : ~k;
   double x;
@@ -420,15 +434,35 @@ __device__ __forceinline__ uint32_t dev_apply(const uint32_t* cols, uint32_t v) 
   return r;
 }
 
-// One thread per 4 KiB chunk: slicing-by-8 register from zero over the chunk,
-// carried over the bytes after it, xor-accumulated per payload.
+// Slicing-by-8 step over 8 bytes (two little-endian words).
+__device__ __forceinline__ uint32_t crc_step8(const uint32_t (*tab)[256], uint32_t s, uint32_t lo,
+                                              uint32_t hi) {
+  const uint32_t a = s ^ lo;
+  return tab[7][a & 0xFF] ^ tab[6][(a >> 8) & 0xFF] ^ tab[5][(a >> 16) & 0xFF] ^
+         tab[4][a >> 24] ^ tab[3][hi & 0xFF] ^ tab[2][(hi >> 8) & 0xFF] ^
+         tab[1][(hi >> 16) & 0xFF] ^ tab[0][hi >> 24];
+}
+
+__device__ __forceinline__ uint32_t crc_step16(const uint32_t (*tab)[256], uint32_t s,
+                                               const uint4& x) {
+  return crc_step8(tab, crc_step8(tab, s, x.x, x.y), x.z, x.w);
+}
+
+// Four threads per 4 KiB chunk, one per 1 KiB quarter: each runs the
+// slicing-by-8 register from zero over its quarter and carries it to the
+// chunk's end with the 3/2/1 KiB zero-byte map; two shuffles join the
+// quarters; the first lane carries the chunk to its payload's end (binary
+// powers of the whole-chunk map, then the last chunk's length) and the
+// payload registers are xor-accumulated.  A payload's short last chunk is
+// run by its first lane alone.  pw holds kCrcPowers maps for 2^j whole
+// chunks, then the three quarter maps.
 __global__ void __launch_bounds__(256) k_crc32c(const uint8_t* __restrict__ base,
                                                 const CrcJob* __restrict__ jobs, int n_jobs,
                                                 int64_t total_chunks,
                                                 const uint32_t* __restrict__ pw,
                                                 uint32_t* __restrict__ out) {
   __shared__ uint32_t tab[8][256];
-  __shared__ uint32_t spw[kCrcPowers][32];
+  __shared__ uint32_t spw[kCrcPowers + 3][32];
   const int tid = threadIdx.x;
   {
     uint32_t c = (uint32_t)tid;
@@ -440,44 +474,77 @@ __global__ void __launch_bounds__(256) k_crc32c(const uint8_t* __restrict__ base
     tab[k][tid] = (tab[k - 1][tid] >> 8) ^ tab[0][tab[k - 1][tid] & 0xFF];
     __syncthreads();
   }
-  for (int i = tid; i < kCrcPowers * 32; i += blockDim.x) spw[i / 32][i % 32] = pw[i];
+  for (int i = tid; i < (kCrcPowers + 3) * 32; i += blockDim.x) spw[i / 32][i % 32] = pw[i];
   __syncthreads();
-  for (int64_t g = (int64_t)blockIdx.x * blockDim.x + tid; g < total_chunks;
-       g += (int64_t)gridDim.x * blockDim.x) {
-    int lo = 0, hi = n_jobs - 1;  // last job with first_chunk <= g
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (jobs[mid].first_chunk <= g) lo = mid;
-      else hi = mid - 1;
-    }
-    const CrcJob& J = jobs[lo];
-    const int64_t i = g - J.first_chunk;
-    const int64_t k = (J.n + kCrcChunk - 1) >> kCrcChunkLog;
-    const int64_t len = (i == k - 1) ? J.n - i * kCrcChunk : kCrcChunk;
-    const uint8_t* p = base + J.off + i * kCrcChunk;
+  const int lane = tid & 31;
+  constexpr int Q = (int)(kCrcChunk / 64);  // uint4 words per quarter
+  const int64_t total = total_chunks * 4;
+  // every lane of a warp runs the same iterations (shuffles and the xor scan
+  // need the whole warp); lanes past the end carry job -1
+  for (int64_t t0 = (int64_t)blockIdx.x * blockDim.x + (tid & ~31); t0 < total;
+       t0 += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t gt = t0 + lane, g = gt >> 2;
+    const int q = (int)(gt & 3);
+    int lo = -1;
     uint32_t s = 0;
-    const int64_t words = len >> 4;
-    const uint4* q = reinterpret_cast<const uint4*>(p);
-    for (int64_t w = 0; w < words; w++) {
-      const uint4 x = __ldg(q + w);
-      uint32_t a = s ^ x.x;
-      s = tab[7][a & 0xFF] ^ tab[6][(a >> 8) & 0xFF] ^ tab[5][(a >> 16) & 0xFF] ^
-          tab[4][a >> 24] ^ tab[3][x.y & 0xFF] ^ tab[2][(x.y >> 8) & 0xFF] ^
-          tab[1][(x.y >> 16) & 0xFF] ^ tab[0][x.y >> 24];
-      a = s ^ x.z;
-      s = tab[7][a & 0xFF] ^ tab[6][(a >> 8) & 0xFF] ^ tab[5][(a >> 16) & 0xFF] ^
-          tab[4][a >> 24] ^ tab[3][x.w & 0xFF] ^ tab[2][(x.w >> 8) & 0xFF] ^
-          tab[1][(x.w >> 16) & 0xFF] ^ tab[0][x.w >> 24];
+    int64_t i = 0, k = 0;
+    if (gt < total) {
+      int hi = n_jobs - 1;  // last job with first_chunk <= g
+      lo = 0;
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (jobs[mid].first_chunk <= g) lo = mid;
+        else hi = mid - 1;
+      }
+      const CrcJob& J = jobs[lo];
+      i = g - J.first_chunk;
+      k = (J.n + kCrcChunk - 1) >> kCrcChunkLog;
+      const int64_t len = (i == k - 1) ? J.n - i * kCrcChunk : kCrcChunk;
+      const uint8_t* p = base + J.off + i * kCrcChunk;
+      const uint4* w4 = reinterpret_cast<const uint4*>(p);
+      if (len == kCrcChunk) {
+        const uint4* qq = w4 + q * Q;
+        uint32_t r = 0;
+#pragma unroll 4
+        for (int w = 0; w < Q; w++) r = crc_step16(tab, r, __ldg(qq + w));
+        s = q < 3 ? dev_apply(spw[kCrcPowers + 2 - q], r) : r;
+      } else if (q == 0) {
+        const int64_t words = len >> 4;
+        for (int64_t w = 0; w < words; w++) s = crc_step16(tab, s, __ldg(w4 + w));
+        for (int64_t j = words << 4; j < len; j++) s = (s >> 8) ^ tab[0][(s ^ p[j]) & 0xFF];
+      }
     }
-    for (int64_t j = words << 4; j < len; j++) s = (s >> 8) ^ tab[0][(s ^ p[j]) & 0xFF];
-    if (i < k - 1) {
+    s ^= __shfl_xor_sync(0xFFFFFFFFu, s, 1);  // the four quarters of one chunk
+    s ^= __shfl_xor_sync(0xFFFFFFFFu, s, 2);
+    if (q != 0) s = 0;
+    if (lo >= 0 && q == 0 && i < k - 1) {
       const int64_t m = k - 2 - i;  // whole chunks between this one and the last
       for (int j = 0; j < kCrcPowers; j++)
         if ((m >> j) & 1) s = dev_apply(spw[j], s);
-      s = dev_apply(J.last, s);
+      s = dev_apply(jobs[lo].last, s);
     }
-    atomicXor(out + lo, s);
+    // Chunks of one payload are consecutive lanes: an inclusive xor scan within
+    // each run of equal jobs leaves the run's total in its last lane, which
+    // alone issues the atomic (same-address atomics serialise in L2).
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, s, o);
+      const int tj = __shfl_up_sync(0xFFFFFFFFu, lo, o);
+      if (lane >= o && tj == lo) s ^= t;
+    }
+    const int next = __shfl_down_sync(0xFFFFFFFFu, lo, 1);
+    if (lo >= 0 && (lane == 31 || next != lo)) atomicXor(out + lo, s);
   }
+}
+
+// kCrcPowers maps for 2^j whole chunks, then the maps for 1, 2, 3 quarters.
+std::vector<uint32_t> crc_device_maps() {
+  std::vector<uint32_t> pw((kCrcPowers + 3) * 32);
+  const ZeroOps& Z = zero_ops();
+  for (int j = 0; j < kCrcPowers; j++) memcpy(&pw[j * 32], Z.pw[kCrcChunkLog + j].c, 128);
+  for (int q = 1; q <= 3; q++)
+    memcpy(&pw[(kCrcPowers + q - 1) * 32], zeros_op((uint64_t)q * (kCrcChunk / 4)).c, 128);
+  return pw;
 }
 
 struct BlockDesc {
@@ -487,70 +554,130 @@ struct BlockDesc {
   int32_t pad;
 };
 
-__global__ void k_oskar_init_extrema(unsigned long long* __restrict__ gm,
-                                     unsigned long long* __restrict__ blw, int32_t nb,
+__global__ void k_oskar_init_extrema(unsigned long long* __restrict__ blw, int32_t nb,
                                      unsigned long long kmax, unsigned long long kmin) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < 6) gm[i] = i < 3 ? kmax : kmin;
   if (i < nb) {
     blw[2 * i] = kmax;
     blw[2 * i + 1] = kmin;
   }
 }
 
-// Grid: x over (channel, baseline) columns, y over blocks.  Each thread walks
-// its column's times: reads are coalesced over baselines, each point's 64
-// amplitude bytes and 24 u,v,w bytes are written contiguously.
-__global__ void __launch_bounds__(256) k_oskar_reshuffle(
-    const uint8_t* __restrict__ raw, const BlockDesc* __restrict__ blocks,
+// Tiled transpose through shared memory, persistent: each CTA walks work
+// items (block, channel, tile of 32 baselines).  For an item it walks the
+// block's times in groups of 8: the group's amplitudes (8 x 32 points x 64 B,
+// 2 KiB contiguous per time) and u,v,w (256 B contiguous per time and
+// component) are read coalesced, then each warp writes one baseline's 8 times
+// (512 B of amplitudes and 192 B of u,v,w contiguous for one channel).  The
+// u/v/w extrema of a CTA go to its own slot of gm (6 keys; the host reduces
+// the slots): same-address atomics from every CTA would serialise in L2.
+constexpr int kRT = 8;   // times per group
+constexpr int kRB = 32;  // baselines per tile
+
+__global__ void __launch_bounds__(256, 4) k_oskar_reshuffle(
+    const uint8_t* __restrict__ raw, const BlockDesc* __restrict__ blocks, int32_t n_blocks,
     const double* __restrict__ invl, int32_t nb, int32_t nc, int32_t T,
     double* __restrict__ amps, double* __restrict__ uvws, unsigned long long* __restrict__ gm,
     unsigned long long* __restrict__ blw) {
-  const BlockDesc bd = blocks[blockIdx.y];
-  const double2* A = reinterpret_cast<const double2*>(raw + bd.amp);
-  const double* U = reinterpret_cast<const double*>(raw + bd.u);
-  const double* V = reinterpret_cast<const double*>(raw + bd.v);
-  const double* W = reinterpret_cast<const double*>(raw + bd.w);
-  double mx[3] = {-1e12, -1e12, -1e12}, mn[3] = {1e12, 1e12, 1e12};
-  const int64_t cols = (int64_t)nb * nc;
-  for (int64_t col = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; col < cols;
-       col += (int64_t)gridDim.x * blockDim.x) {
-    const int32_t c = (int32_t)(col / nb), b = (int32_t)(col - (int64_t)c * nb);
+  // rows padded so the transposed reads are free of bank conflicts: one
+  // baseline (64 B) per time row of amplitudes, one double per row of u,v,w
+  __shared__ double2 sa[kRT][kRB + 1][4];
+  __shared__ double su[3][kRT][kRB + 1];
+  __shared__ unsigned long long red[6][8];
+  const int tiles = (nb + kRB - 1) / kRB;
+  const int64_t items = (int64_t)n_blocks * nc * tiles;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  unsigned long long mx[3] = {0ull, 0ull, 0ull}, mn[3] = {~0ull, ~0ull, ~0ull};
+  for (int64_t item = blockIdx.x; item < items; item += gridDim.x) {
+    const int blk = (int)(item / ((int64_t)nc * tiles));
+    const int rem = (int)(item - (int64_t)blk * nc * tiles);
+    const int c = rem / tiles;
+    const int b0 = (rem - c * tiles) * kRB;
+    const BlockDesc bd = blocks[blk];
+    const double2* A = reinterpret_cast<const double2*>(raw + bd.amp);
+    const double* UVW[3] = {reinterpret_cast<const double*>(raw + bd.u),
+                            reinterpret_cast<const double*>(raw + bd.v),
+                            reinterpret_cast<const double*>(raw + bd.w)};
     const double il = invl[bd.il + c];
-    double wmax = -1e12, wmin = 1e12;
-    for (int32_t t = 0; t < bd.nt; t++) {
-      const int64_t q = ((int64_t)t * nc + c) * nb + b;
-      const int64_t p = ((int64_t)T * b + bd.t0 + t) * nc + c;
-      double2* dst = reinterpret_cast<double2*>(amps + 8 * p);
+    unsigned long long wmax[kRB / 8], wmin[kRB / 8];  // this warp's baselines
 #pragma unroll
-      for (int k = 0; k < 4; k++) dst[k] = __ldg(A + 4 * q + k);
-      const int64_t j = (int64_t)t * nb + b;
-      const double u = __ldg(U + j) * il, v = __ldg(V + j) * il, w = __ldg(W + j) * il;
-      uvws[3 * p] = u;
-      uvws[3 * p + 1] = v;
-      uvws[3 * p + 2] = w;
-      mx[0] = fmax(mx[0], u);
-      mx[1] = fmax(mx[1], v);
-      mx[2] = fmax(mx[2], w);
-      mn[0] = fmin(mn[0], u);
-      mn[1] = fmin(mn[1], v);
-      mn[2] = fmin(mn[2], w);
-      wmax = fmax(wmax, w);
-      wmin = fmin(wmin, w);
+    for (int i = 0; i < kRB / 8; i++) {
+      wmax[i] = 0ull;
+      wmin[i] = ~0ull;
     }
-    if (bd.nt > 0) {
-      atomicMax(blw + 2 * b, order_key(wmax));
-      atomicMin(blw + 2 * b + 1, order_key(wmin));
+    for (int g0 = 0; g0 < bd.nt; g0 += kRT) {
+      const int gn = min(kRT, bd.nt - g0);
+#pragma unroll
+      for (int it = 0; it < kRT * kRB * 4 / 256; it++) {  // amplitudes, 16 B per thread
+        const int e = it * 256 + tid, t = e / (kRB * 4), r = e - t * (kRB * 4);
+        const int b = r >> 2, k = r & 3;
+        if (t < gn && b0 + b < nb)
+          sa[t][b][k] = __ldg(A + 4 * (((int64_t)(g0 + t) * nc + c) * nb + b0 + b) + k);
+      }
+      {
+        const int t = tid / kRB, b = tid - t * kRB;  // 256 threads = 8 times x 32 baselines
+        if (t < gn && b0 + b < nb) {
+          const int64_t j = (int64_t)(g0 + t) * nb + b0 + b;
+#pragma unroll
+          for (int k = 0; k < 3; k++) su[k][t][b] = __ldg(UVW[k] + j) * il;
+        }
+      }
+      __syncthreads();
+#pragma unroll
+      for (int it = 0; it < kRB / 8; it++) {
+        const int b = it * 8 + warp;
+        if (b0 + b < nb) {
+          const int64_t row = (int64_t)T * (b0 + b) + bd.t0 + g0;  // point (b, first time)
+          {
+            const int t = lane >> 2, k = lane & 3;
+            if (t < gn)
+              reinterpret_cast<double2*>(amps)[4 * ((row + t) * nc + c) + k] = sa[t][b][k];
+          }
+          if (lane < 3 * kRT) {
+            const int t = lane / 3, k = lane - 3 * t;
+            if (t < gn) {
+              const double x = su[k][t][b];
+              uvws[3 * ((row + t) * nc + c) + k] = x;
+              const unsigned long long kx = key_for_max(x), kn = key_for_min(x);
+              // constant indices only: a lane-dependent index would put the
+              // accumulators in local memory
+#pragma unroll
+              for (int q = 0; q < 3; q++)
+                if (q == k) {
+                  mx[q] = max(mx[q], kx);
+                  mn[q] = min(mn[q], kn);
+                }
+              if (k == 2) {
+                wmax[it] = max(wmax[it], kx);
+                wmin[it] = min(wmin[it], kn);
+              }
+            }
+          }
+        }
+      }
+      __syncthreads();
+    }
+    // per-baseline w extrema: reduce over the warp, one atomic pair per baseline
+#pragma unroll
+    for (int it = 0; it < kRB / 8; it++) {
+      unsigned long long a = wmax[it], m = wmin[it];
+      for (int o = 16; o; o >>= 1) {
+        a = max(a, __shfl_xor_sync(0xFFFFFFFFu, a, o));
+        m = min(m, __shfl_xor_sync(0xFFFFFFFFu, m, o));
+      }
+      const int b = b0 + it * 8 + warp;
+      if (lane == 0 && b < nb && bd.nt > 0) {
+        atomicMax(blw + 2 * b, a);
+        atomicMin(blw + 2 * b + 1, m);
+      }
     }
   }
-  // CTA reduction of the six extrema, then one atomic each
-  __shared__ double red[6][8];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  // CTA reduction of the six global extrema into this CTA's slot
 #pragma unroll
   for (int k = 0; k < 3; k++) {
     for (int o = 16; o; o >>= 1) {
-      mx[k] = fmax(mx[k], __shfl_xor_sync(0xFFFFFFFFu, mx[k], o));
-      mn[k] = fmin(mn[k], __shfl_xor_sync(0xFFFFFFFFu, mn[k], o));
+      mx[k] = max(mx[k], __shfl_xor_sync(0xFFFFFFFFu, mx[k], o));
+      mn[k] = min(mn[k], __shfl_xor_sync(0xFFFFFFFFu, mn[k], o));
     }
   }
   if (lane == 0) {
@@ -561,12 +688,10 @@ __global__ void __launch_bounds__(256) k_oskar_reshuffle(
     }
   }
   __syncthreads();
-  if (threadIdx.x < 6) {
-    const int k = threadIdx.x;
-    double r = red[k][0];
-    for (int i = 1; i < (int)(blockDim.x >> 5); i++) r = k < 3 ? fmax(r, red[k][i]) : fmin(r, red[k][i]);
-    if (k < 3) atomicMax(gm + k, order_key(r));
-    else atomicMin(gm + k, order_key(r));
+  if (tid < 6) {
+    unsigned long long r = red[tid][0];
+    for (int i = 1; i < 8; i++) r = tid < 3 ? max(r, red[tid][i]) : min(r, red[tid][i]);
+    gm[6 * (int64_t)blockIdx.x + tid] = r;
   }
 }
 
@@ -647,7 +772,7 @@ int stream_pieces(int fd, const std::vector<Piece>& pieces, uint8_t* d_raw) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return GB_ERR_CUDA;
   const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
-  const int K = (int)std::min<size_t>(pieces.size(), std::min(8u, std::max(1u, hw / 2)));
+  const int K = (int)std::min<size_t>(pieces.size(), std::min(16u, hw));
   std::atomic<size_t> next{0};
   std::atomic<int> err{0};
   auto worker = [&]() {
@@ -857,27 +982,29 @@ int ingest(const VisData* vd, double* d_amps, double* d_uvws, Metrix* mp, WMaxMi
   std::vector<DevJob> jobs;
   for (const DevJob& j : in.jobs)
     if (j.seq < in.first_err_seq) jobs.push_back(j);
+  const int tiles = (nb + kRB - 1) / kRB;
+  const int64_t items = (int64_t)in.blocks.size() * nc * tiles;
+  int per_sm = 0;  // persistent: as many CTAs as fit at once
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_oskar_reshuffle, 256, 0) !=
+          cudaSuccess || per_sm < 1)
+    per_sm = 1;
+  const int n_cta = (int)std::min<int64_t>(items, (int64_t)gb::sm_count() * per_sm);
   const int64_t gm_off = align256(in.raw_bytes);
-  const int64_t blw_off = gm_off + 256;
+  const int64_t blw_off = align256(gm_off + (int64_t)n_cta * 48);
   const int64_t crc_off = align256(blw_off + (int64_t)std::max(nb, 0) * 16);
   const int64_t job_off = align256(crc_off + (int64_t)jobs.size() * 4);
   const int64_t pw_off = align256(job_off + (int64_t)jobs.size() * sizeof(CrcJob));
-  const int64_t blk_off = align256(pw_off + kCrcPowers * 32 * 4);
+  const int64_t blk_off = align256(pw_off + (kCrcPowers + 3) * 32 * 4);
   const int64_t il_off = align256(blk_off + (int64_t)in.blocks.size() * sizeof(BlockDesc));
   const int64_t total = align256(il_off + (int64_t)in.invl.size() * 8);
   uint8_t* d = nullptr;
-  std::vector<unsigned long long> keys(6 + 2 * (size_t)std::max(nb, 0));
+  std::vector<unsigned long long> part(6 * (size_t)n_cta), keys(2 * (size_t)std::max(nb, 0));
   std::vector<uint32_t> crc_out(jobs.size());
   std::vector<CrcJob> cj(jobs.size());
-  std::vector<uint32_t> pw(kCrcPowers * 32);
+  const std::vector<uint32_t> pw = crc_device_maps();
   std::vector<Piece> pieces;
   int64_t chunks = 0;
   int crc_fail_seq = INT_MAX;
-  {
-    const ZeroOps& Z = zero_ops();
-    for (int j = 0; j < kCrcPowers; j++)
-      memcpy(&pw[j * 32], Z.pw[kCrcChunkLog + j].c, 128);
-  }
   for (size_t j = 0; j < jobs.size(); j++) {
     const DevJob& J = jobs[j];
     cj[j].off = J.dev_off;
@@ -913,34 +1040,34 @@ int ingest(const VisData* vd, double* d_amps, double* d_uvws, Metrix* mp, WMaxMi
   OSK_CUDA(cudaEventRecord(ev[0], s), "cudaEventRecord");
   {
     const unsigned long long kmax = host_key(-1e12), kmin = host_key(1e12);
-    const int64_t ninit = std::max<int64_t>(6, nb);
-    k_oskar_init_extrema<<<(unsigned)((ninit + 255) / 256), 256, 0, s>>>(
-        (unsigned long long*)(d + gm_off), (unsigned long long*)(d + blw_off), nb, kmax, kmin);
-    OSK_CUDA(cudaGetLastError(), "k_oskar_init_extrema");
+    if (nb > 0) {
+      k_oskar_init_extrema<<<(unsigned)((nb + 255) / 256), 256, 0, s>>>(
+          (unsigned long long*)(d + blw_off), nb, kmax, kmin);
+      OSK_CUDA(cudaGetLastError(), "k_oskar_init_extrema");
+    }
   }
   if (chunks > 0) {
-    const int64_t grid = std::min<int64_t>((chunks + 255) / 256, (int64_t)gb::sm_count() * 64);
+    const int64_t grid =
+        std::min<int64_t>((4 * chunks + 255) / 256, (int64_t)gb::sm_count() * 64);
     k_crc32c<<<(unsigned)grid, 256, 0, s>>>(d, (const CrcJob*)(d + job_off), (int)jobs.size(),
                                             chunks, (const uint32_t*)(d + pw_off),
                                             (uint32_t*)(d + crc_off));
     OSK_CUDA(cudaGetLastError(), "k_crc32c");
   }
   OSK_CUDA(cudaEventRecord(ev[1], s), "cudaEventRecord");
-  if (!in.blocks.empty() && (int64_t)nb * nc > 0) {
-    const int64_t cols = (int64_t)nb * nc;
-    const unsigned gx = (unsigned)std::min<int64_t>((cols + 255) / 256, 65535);
-    for (size_t b0 = 0; b0 < in.blocks.size(); b0 += 65535) {
-      const unsigned gy = (unsigned)std::min<size_t>(in.blocks.size() - b0, 65535);
-      k_oskar_reshuffle<<<dim3(gx, gy), 256, 0, s>>>(
-          d, (const BlockDesc*)(d + blk_off) + b0, (const double*)(d + il_off), nb, nc, T, d_amps,
-          d_uvws, (unsigned long long*)(d + gm_off), (unsigned long long*)(d + blw_off));
-      OSK_CUDA(cudaGetLastError(), "k_oskar_reshuffle");
-    }
+  if (n_cta > 0) {
+    k_oskar_reshuffle<<<(unsigned)n_cta, 256, 0, s>>>(
+        d, (const BlockDesc*)(d + blk_off), (int32_t)in.blocks.size(),
+        (const double*)(d + il_off), nb, nc, T, d_amps, d_uvws,
+        (unsigned long long*)(d + gm_off), (unsigned long long*)(d + blw_off));
+    OSK_CUDA(cudaGetLastError(), "k_oskar_reshuffle");
   }
   OSK_CUDA(cudaEventRecord(ev[2], s), "cudaEventRecord");
-  OSK_CUDA(cudaMemcpyAsync(keys.data(), d + gm_off, 48, cudaMemcpyDeviceToHost, s), "D2H");
+  if (n_cta > 0)
+    OSK_CUDA(cudaMemcpyAsync(part.data(), d + gm_off, part.size() * 8, cudaMemcpyDeviceToHost,
+                             s), "D2H");
   if (nb > 0)
-    OSK_CUDA(cudaMemcpyAsync(keys.data() + 6, d + blw_off, (size_t)nb * 16,
+    OSK_CUDA(cudaMemcpyAsync(keys.data(), d + blw_off, (size_t)nb * 16,
                              cudaMemcpyDeviceToHost, s), "D2H");
   if (!jobs.empty())
     OSK_CUDA(cudaMemcpyAsync(crc_out.data(), d + crc_off, jobs.size() * 4,
@@ -967,17 +1094,23 @@ int ingest(const VisData* vd, double* d_amps, double* d_uvws, Metrix* mp, WMaxMi
     rc = in.first_err;
   }
   if (mp) {
-    mp->maxu = key_value(keys[0]);
-    mp->maxv = key_value(keys[1]);
-    mp->maxw = key_value(keys[2]);
-    mp->minu = key_value(keys[3]);
-    mp->minv = key_value(keys[4]);
-    mp->minw = key_value(keys[5]);
+    // the reference's start values -1e12 / 1e12 take part like any value
+    unsigned long long g[6] = {host_key(-1e12), host_key(-1e12), host_key(-1e12),
+                               host_key(1e12), host_key(1e12), host_key(1e12)};
+    for (int c = 0; c < n_cta; c++)
+      for (int k = 0; k < 6; k++)
+        g[k] = k < 3 ? std::max(g[k], part[6 * c + k]) : std::min(g[k], part[6 * c + k]);
+    mp->maxu = key_value(g[0]);
+    mp->maxv = key_value(g[1]);
+    mp->maxw = key_value(g[2]);
+    mp->minu = key_value(g[3]);
+    mp->minv = key_value(g[4]);
+    mp->minw = key_value(g[5]);
   }
   if (bl_ws)
     for (int i = 0; i < nb; i++) {
-      bl_ws[i].maxw = key_value(keys[6 + 2 * i]);
-      bl_ws[i].minw = key_value(keys[7 + 2 * i]);
+      bl_ws[i].maxw = key_value(keys[2 * i]);
+      bl_ws[i].minw = key_value(keys[2 * i + 1]);
     }
 done:
   if (d) {
@@ -1196,9 +1329,7 @@ extern "C" int gb_crc32c_device(const void* d_data, int64_t n, uint32_t code, ui
   job.n = n;
   job.first_chunk = 0;
   memcpy(job.last, zeros_op((uint64_t)(n - (k - 1) * kCrcChunk)).c, 128);
-  std::vector<uint32_t> pw(kCrcPowers * 32);
-  const ZeroOps& Z = zero_ops();
-  for (int j = 0; j < kCrcPowers; j++) memcpy(&pw[j * 32], Z.pw[kCrcChunkLog + j].c, 128);
+  const std::vector<uint32_t> pw = crc_device_maps();
   uint8_t* d = nullptr;
   uint32_t r = 0;
   int rc = 0;
@@ -1209,7 +1340,7 @@ extern "C" int gb_crc32c_device(const void* d_data, int64_t n, uint32_t code, ui
   OSK_CUDA(cudaMemcpyAsync(d + 256 + sizeof(CrcJob), pw.data(), pw.size() * 4,
                            cudaMemcpyHostToDevice, s), "H2D");
   {
-    const int64_t grid = std::min<int64_t>((k + 255) / 256, (int64_t)gb::sm_count() * 64);
+    const int64_t grid = std::min<int64_t>((4 * k + 255) / 256, (int64_t)gb::sm_count() * 64);
     k_crc32c<<<(unsigned)grid, 256, 0, s>>>((const uint8_t*)d_data, (const CrcJob*)(d + 256), 1,
                                             k, (const uint32_t*)(d + 256 + sizeof(CrcJob)),
                                             (uint32_t*)d);
