@@ -78,12 +78,19 @@ struct __align__(16) GridRec {
   int32_t xm, ym; // piece corner mod P
   int32_t wx, wy; // piece extent
   int32_t pitch;  // GCF row pitch (the plane's support S)
-  int32_t P;      // period of the run
+  int32_t P;      // period of the run, | kWholePiece when the piece is P x P
 };
 
+constexpr int32_t kWholePiece = 1 << 16;
+
 struct __align__(16) DegridRec {
-  int32_t gcf, q0, wx, wy, pitch, vis, cut, pad;
+  int32_t gcf, q0, pitch, vis;
+  int16_t wx, wy;  // piece extent
+  int16_t dj, di;  // a sub-warp's stride through the piece: SW taps = dj rows + di columns
+  float rcp_wx;    // 1 / wx, for each lane's first tap without an integer division
+  int32_t cut;     // footprint cut into pieces: accumulate with atomics
 };
+static_assert(sizeof(DegridRec) == 32, "DegridRec is two 16-byte words");
 
 // Residue slots a thread needs for period P in a group of L threads.
 __device__ __forceinline__ int slots_for(int P, int L) { return (P * P + L - 1) / L; }
@@ -91,18 +98,22 @@ __device__ __forceinline__ int slots_for(int P, int L) { return (P * P + L - 1) 
 // One run [k, e) of equal period P of the staged batch: thread lt owns the
 // residues rr = lt + m L < P^2, (a, b) = (rr mod P, rr div P); U pieces at a
 // time, all GCF loads first, then the read-modify-writes in piece order.
-template <int R, int U>
+// FULL: every piece of the run is a whole P x P square, so every owned
+// residue has a tap and the extent checks drop out.
+template <int R, int U, bool FULL>
 __device__ __forceinline__ void grid_run(int k, int e, int lt, int L, int A,
                                          const GridRec* __restrict__ srec,
                                          const float2* __restrict__ svis,
                                          float4* __restrict__ acc,
                                          const float2* __restrict__ gcf) {
-  const int P = srec[k].P;
+  const int P = srec[k].P & 0xFFFF;
   int ra[R], rb[R];
+  bool own[R];  // slot m holds a residue (R L may exceed P^2)
 #pragma unroll
   for (int m = 0; m < R; m++) {
     const int rr = lt + m * L;
-    if (rr < P * P) {
+    own[m] = rr < P * P;
+    if (own[m]) {
       rb[m] = rr / P;
       ra[m] = rr - rb[m] * P;
     } else {
@@ -125,7 +136,7 @@ __device__ __forceinline__ void grid_run(int k, int e, int lt, int L, int A,
         i += i < 0 ? P : 0;
         int j = rb[m] - r.ym;
         j += j < 0 ? P : 0;
-        if (live && i < r.wx && j < r.wy) {
+        if (live && own[m] && (FULL || (i < r.wx && j < r.wy))) {
           c[u][m] = __ldg(gcf + r.gcf + j * r.pitch + i);
           qi[u][m] = r.q0 + j * A + i;
         } else {
@@ -149,6 +160,23 @@ __device__ __forceinline__ void grid_run(int k, int e, int lt, int L, int A,
         }
       }
     }
+  }
+}
+
+template <bool FULL>
+__device__ __forceinline__ void grid_dispatch(int slots, int k, int e, int lt, int L, int A,
+                                              const GridRec* __restrict__ srec,
+                                              const float2* __restrict__ svis,
+                                              float4* __restrict__ acc,
+                                              const float2* __restrict__ gcf) {
+  switch (slots) {
+    case 1: grid_run<1, 8, FULL>(k, e, lt, L, A, srec, svis, acc, gcf); break;
+    case 2: grid_run<2, 4, FULL>(k, e, lt, L, A, srec, svis, acc, gcf); break;
+    case 3: grid_run<3, 3, FULL>(k, e, lt, L, A, srec, svis, acc, gcf); break;
+    case 4: grid_run<4, 2, FULL>(k, e, lt, L, A, srec, svis, acc, gcf); break;
+    case 5:
+    case 6: grid_run<6, 1, FULL>(k, e, lt, L, A, srec, svis, acc, gcf); break;
+    default: grid_run<8, 1, FULL>(k, e, lt, L, A, srec, svis, acc, gcf); break;
   }
 }
 
@@ -177,30 +205,28 @@ __device__ __forceinline__ void grid_item(const TiledArgs& a, const Item& it, in
       d.wx = r.wx;
       d.wy = r.wy;
       d.pitch = r.sm1 + 1;
-      d.P = r.pm1 + 1;
+      d.P = (r.pm1 + 1) | (r.wx == r.pm1 + 1 && r.wy == r.pm1 + 1 ? kWholePiece : 0);
       srec[lt] = d;
       svis[lt] = __ldg(vis + r.vis);
     }
     group_sync(bar, L, whole);
     int k = 0;
     while (k < nb) {
-      const int P = srec[k].P;
+      const int P = srec[k].P & 0xFFFF;
       if (P != curP) {
         // the residue map changes: finish every read-modify-write of the old one
         group_sync(bar, L, whole);
         curP = P;
       }
-      int e = k + 1;
-      while (e < nb && srec[e].P == P) e++;
-      switch (slots_for(P, L)) {
-        case 1: grid_run<1, 8>(k, e, lt, L, A, srec, svis, acc, gcf); break;
-        case 2: grid_run<2, 4>(k, e, lt, L, A, srec, svis, acc, gcf); break;
-        case 3: grid_run<3, 3>(k, e, lt, L, A, srec, svis, acc, gcf); break;
-        case 4: grid_run<4, 2>(k, e, lt, L, A, srec, svis, acc, gcf); break;
-        case 5:
-        case 6: grid_run<6, 1>(k, e, lt, L, A, srec, svis, acc, gcf); break;
-        default: grid_run<8, 1>(k, e, lt, L, A, srec, svis, acc, gcf); break;
+      int e = k;
+      bool full = true;
+      for (; e < nb; e++) {
+        const int pe = srec[e].P;
+        if ((pe & 0xFFFF) != P) break;
+        full = full && (pe & kWholePiece);
       }
+      if (full) grid_dispatch<true>(slots_for(P, L), k, e, lt, L, A, srec, svis, acc, gcf);
+      else grid_dispatch<false>(slots_for(P, L), k, e, lt, L, A, srec, svis, acc, gcf);
       k = e;
     }
   }
@@ -277,12 +303,14 @@ __device__ __forceinline__ void degrid_item(const TiledArgs& a, const Item& it, 
       DegridRec d;
       d.gcf = (int32_t)r.gcf;
       d.q0 = r.yl * A + r.xl;
-      d.wx = r.wx;
-      d.wy = r.wy;
       d.pitch = r.sm1 + 1;
       d.vis = r.vis;
+      d.wx = r.wx;
+      d.wy = r.wy;
+      d.dj = (int16_t)(SW / r.wx);
+      d.di = (int16_t)(SW - d.dj * r.wx);
+      d.rcp_wx = 1.0f / (float)r.wx;
       d.cut = r.sm1 > r.pm1;
-      d.pad = 0;
       srec[lt] = d;
     }
     group_sync(bar, L, whole);
@@ -295,9 +323,11 @@ __device__ __forceinline__ void degrid_item(const TiledArgs& a, const Item& it, 
         const float2* gp = gcf + r.gcf;
         const float2* sp = sg + r.q0;
         const int wx = r.wx;
-        int j = sl / wx;
+        // sl / wx: (sl + 1/2) / wx is at least 1/(2 wx) from an integer, far
+        // more than the float rounding of the product
+        int j = (int)(((float)sl + 0.5f) * r.rcp_wx);
         int i = sl - j * wx;
-        const int dj = SW / wx, di = SW - dj * wx;
+        const int dj = r.dj, di = r.di;
 #pragma unroll 4
         for (; j < r.wy;) {
           const float2 c = __ldg(gp + j * r.pitch + i);
