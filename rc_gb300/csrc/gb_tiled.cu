@@ -86,10 +86,12 @@ constexpr int32_t kWholePiece = 1 << 16;
 struct __align__(16) DegridRec {
   int32_t gcf, q0, pitch, vis;
   int16_t wx, wy;  // piece extent
-  int16_t dj, di;  // a sub-warp's stride through the piece: SW taps = dj rows + di columns
-  float rcp_wx;    // 1 / wx, for each lane's first tap without an integer division
-  int32_t cut;     // footprint cut into pieces: accumulate with atomics
+  int16_t dj, di;  // a sub-warp's stride through the piece: SW steps = dj rows + di steps
+  float rcp_w;     // 1 / (steps per row), for each lane's first step without a division
+  int32_t flags;   // kRecCut: footprint cut into pieces (accumulate with atomics);
+                   // kRecPaired: a step is two adjacent taps (one 16-byte GCF load)
 };
+constexpr int32_t kRecCut = 1, kRecPaired = 2;
 static_assert(sizeof(DegridRec) == 32, "DegridRec is two 16-byte words");
 
 // Residue slots a thread needs for period P in a group of L threads.
@@ -292,6 +294,7 @@ __device__ __forceinline__ void degrid_item(const TiledArgs& a, const Item& it, 
                                              : make_float2(0.f, 0.f);
   }
   constexpr int SUBS = 32 / SW;
+  const bool gcf16 = (reinterpret_cast<uintptr_t>(gcf) & 15) == 0;
   const int nw = L >> 5, w = lt >> 5, lane = lt & 31;
   const int sub = lane / SW, sl = lane - sub * SW;
   const int end = it.start + it.count;
@@ -307,10 +310,14 @@ __device__ __forceinline__ void degrid_item(const TiledArgs& a, const Item& it, 
       d.vis = r.vis;
       d.wx = r.wx;
       d.wy = r.wy;
-      d.dj = (int16_t)(SW / r.wx);
-      d.di = (int16_t)(SW - d.dj * r.wx);
-      d.rcp_wx = 1.0f / (float)r.wx;
-      d.cut = r.sm1 > r.pm1;
+      // taps in pairs when the piece's rows, its GCF rows and its first tap
+      // all start on 16-byte boundaries
+      const bool paired = gcf16 && (r.wx & 1) == 0 && (d.pitch & 1) == 0 && (d.gcf & 1) == 0;
+      const int steps = paired ? r.wx >> 1 : r.wx;  // steps per row
+      d.dj = (int16_t)(SW / steps);
+      d.di = (int16_t)(SW - d.dj * steps);
+      d.rcp_w = 1.0f / (float)steps;
+      d.flags = (r.sm1 > r.pm1 ? kRecCut : 0) | (paired ? kRecPaired : 0);
       srec[lt] = d;
     }
     group_sync(bar, L, whole);
@@ -320,33 +327,66 @@ __device__ __forceinline__ void degrid_item(const TiledArgs& a, const Item& it, 
       const DegridRec r = srec[live ? k : kk];
       float ar = 0.f, ai = 0.f, cr = 0.f, ci = 0.f;
       if (live) {
-        const float2* gp = gcf + r.gcf;
         const float2* sp = sg + r.q0;
-        const int wx = r.wx;
-        // sl / wx: (sl + 1/2) / wx is at least 1/(2 wx) from an integer, far
-        // more than the float rounding of the product
-        int j = (int)(((float)sl + 0.5f) * r.rcp_wx);
-        int i = sl - j * wx;
+        // sl / steps: (sl + 1/2) / steps is at least 1/(2 steps) from an
+        // integer, far more than the float rounding of the product
+        int j = (int)(((float)sl + 0.5f) * r.rcp_w);
         const int dj = r.dj, di = r.di;
+        if (r.flags & kRecPaired) {
+          const int w2 = r.wx >> 1, p2 = r.pitch >> 1;
+          const float4* gp = reinterpret_cast<const float4*>(gcf + r.gcf);
+          int i = sl - j * w2;
 #pragma unroll 4
-        for (; j < r.wy;) {
-          const float2 c = __ldg(gp + j * r.pitch + i);
-          const float2 x = sp[j * A + i];
-          float pr, pi;
-          if (MODE == 0) {  // x * conj(c)
-            pr = x.x * c.x + x.y * c.y;
-            pi = x.y * c.x - x.x * c.y;
-          } else {  // -(x * c)
-            pr = -(x.x * c.x - x.y * c.y);
-            pi = -(x.x * c.y + x.y * c.x);
+          for (; j < r.wy;) {
+            const float4 c = __ldg(gp + j * p2 + i);
+            const float2 x0 = sp[j * A + 2 * i], x1 = sp[j * A + 2 * i + 1];
+            float pr0, pi0, pr1, pi1;
+            if (MODE == 0) {  // x * conj(c)
+              pr0 = x0.x * c.x + x0.y * c.y;
+              pi0 = x0.y * c.x - x0.x * c.y;
+              pr1 = x1.x * c.z + x1.y * c.w;
+              pi1 = x1.y * c.z - x1.x * c.w;
+            } else {  // -(x * c)
+              pr0 = -(x0.x * c.x - x0.y * c.y);
+              pi0 = -(x0.x * c.y + x0.y * c.x);
+              pr1 = -(x1.x * c.z - x1.y * c.w);
+              pi1 = -(x1.x * c.w + x1.y * c.z);
+            }
+            kahan(ar, cr, pr0);
+            kahan(ai, ci, pi0);
+            kahan(ar, cr, pr1);
+            kahan(ai, ci, pi1);
+            i += di;
+            j += dj;
+            if (i >= w2) {
+              i -= w2;
+              j++;
+            }
           }
-          kahan(ar, cr, pr);
-          kahan(ai, ci, pi);
-          i += di;
-          j += dj;
-          if (i >= wx) {
-            i -= wx;
-            j++;
+        } else {
+          const float2* gp = gcf + r.gcf;
+          const int wx = r.wx;
+          int i = sl - j * wx;
+#pragma unroll 4
+          for (; j < r.wy;) {
+            const float2 c = __ldg(gp + j * r.pitch + i);
+            const float2 x = sp[j * A + i];
+            float pr, pi;
+            if (MODE == 0) {  // x * conj(c)
+              pr = x.x * c.x + x.y * c.y;
+              pi = x.y * c.x - x.x * c.y;
+            } else {  // -(x * c)
+              pr = -(x.x * c.x - x.y * c.y);
+              pi = -(x.x * c.y + x.y * c.x);
+            }
+            kahan(ar, cr, pr);
+            kahan(ai, ci, pi);
+            i += di;
+            j += dj;
+            if (i >= wx) {
+              i -= wx;
+              j++;
+            }
           }
         }
       }
@@ -358,7 +398,7 @@ __device__ __forceinline__ void degrid_item(const TiledArgs& a, const Item& it, 
         ai += __shfl_xor_sync(0xffffffffu, ai, o);
       }
       if (live && sl == 0) {
-        if (r.cut)
+        if (r.flags & kRecCut)
           atomicAdd(pred + r.vis, make_float2(ar, ai));
         else
           pred[r.vis] = make_float2(ar, ai);
