@@ -287,12 +287,19 @@ __device__ __forceinline__ void degrid_item(const TiledArgs& a, const Item& it, 
   float2* __restrict__ pred = gs.vis;
   const int AA = A * A;
   const int x0 = it.tile_x * a.T, y0 = it.tile_y * a.T;
+  // asynchronous copies straight into shared memory (no register round
+  // trip), all in flight at once; pixels outside the grid are zero-filled
   for (int q = lt; q < AA; q += L) {
     const int py = q / A, px = q - py * A;
     const int gx = x0 + px, gy = y0 + py;
-    sg[q] = (gx < gs.ext_x && gy < gs.ext_y) ? grid[(int64_t)gy * gs.pitch + gx]
-                                             : make_float2(0.f, 0.f);
+    const bool in = gx < gs.ext_x && gy < gs.ext_y;
+    const float2* src = in ? grid + (int64_t)gy * gs.pitch + gx : grid;
+    const unsigned dst = (unsigned)__cvta_generic_to_shared(sg + q);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(dst), "l"(src),
+                 "r"(in ? 8 : 0)
+                 : "memory");
   }
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
   constexpr int SUBS = 32 / SW;
   const bool gcf16 = (reinterpret_cast<uintptr_t>(gcf) & 15) == 0;
   const int nw = L >> 5, w = lt >> 5, lane = lt & 31;
@@ -300,7 +307,7 @@ __device__ __forceinline__ void degrid_item(const TiledArgs& a, const Item& it, 
   const int end = it.start + it.count;
   for (int base = it.start; base < end; base += L) {
     const int nb = min(L, end - base);
-    group_sync(bar, L, whole);  // staging done / previous batch consumed
+    group_sync(bar, L, whole);  // previous batch consumed
     if (lt < nb) {
       const Rec r = a.recs[base + lt];
       DegridRec d;
@@ -320,6 +327,9 @@ __device__ __forceinline__ void degrid_item(const TiledArgs& a, const Item& it, 
       d.flags = (r.sm1 > r.pm1 ? kRecCut : 0) | (paired ? kRecPaired : 0);
       srec[lt] = d;
     }
+    // this thread's staging copies (issued before the first batch's record
+    // loads, so the two latencies overlap); the barrier publishes them all
+    if (base == it.start) asm volatile("cp.async.wait_group 0;\n" ::: "memory");
     group_sync(bar, L, whole);
     for (int kk = w * SUBS; kk < nb; kk += nw * SUBS) {
       const int k = kk + sub;
@@ -336,31 +346,53 @@ __device__ __forceinline__ void degrid_item(const TiledArgs& a, const Item& it, 
           const int w2 = r.wx >> 1, p2 = r.pitch >> 1;
           const float4* gp = reinterpret_cast<const float4*>(gcf + r.gcf);
           int i = sl - j * w2;
-#pragma unroll 4
-          for (; j < r.wy;) {
-            const float4 c = __ldg(gp + j * p2 + i);
-            const float2 x0 = sp[j * A + 2 * i], x1 = sp[j * A + 2 * i + 1];
-            float pr0, pi0, pr1, pi1;
-            if (MODE == 0) {  // x * conj(c)
-              pr0 = x0.x * c.x + x0.y * c.y;
-              pi0 = x0.y * c.x - x0.x * c.y;
-              pr1 = x1.x * c.z + x1.y * c.w;
-              pi1 = x1.y * c.z - x1.x * c.w;
-            } else {  // -(x * c)
-              pr0 = -(x0.x * c.x - x0.y * c.y);
-              pi0 = -(x0.x * c.y + x0.y * c.x);
-              pr1 = -(x1.x * c.z - x1.y * c.w);
-              pi1 = -(x1.x * c.w + x1.y * c.z);
+          // this lane's pairs: sl, sl + SW, ... below w2 * wy (SW is a power of two)
+          const int tot = w2 * r.wy;
+          const int n = tot > sl ? (tot - sl + SW - 1) / SW : 0;
+          constexpr int UN = 4;
+          for (int t = 0; t < n; t += UN) {
+            // positions first, then every load of the group, then the sums
+            int off_g[UN], off_s[UN];
+#pragma unroll
+            for (int u = 0; u < UN; u++) {
+              off_g[u] = j * p2 + i;
+              off_s[u] = j * A + 2 * i;
+              i += di;
+              j += dj;
+              if (i >= w2) {
+                i -= w2;
+                j++;
+              }
             }
-            kahan(ar, cr, pr0);
-            kahan(ai, ci, pi0);
-            kahan(ar, cr, pr1);
-            kahan(ai, ci, pi1);
-            i += di;
-            j += dj;
-            if (i >= w2) {
-              i -= w2;
-              j++;
+            float4 c[UN];
+            float2 x0[UN], x1[UN];
+#pragma unroll
+            for (int u = 0; u < UN; u++) {
+              const bool ok = t + u < n;
+              c[u] = ok ? __ldg(gp + off_g[u]) : make_float4(0.f, 0.f, 0.f, 0.f);
+              x0[u] = ok ? sp[off_s[u]] : make_float2(0.f, 0.f);
+              x1[u] = ok ? sp[off_s[u] + 1] : make_float2(0.f, 0.f);
+            }
+#pragma unroll
+            for (int u = 0; u < UN; u++) {
+              if (t + u < n) {
+                float pr0, pi0, pr1, pi1;
+                if (MODE == 0) {  // x * conj(c)
+                  pr0 = x0[u].x * c[u].x + x0[u].y * c[u].y;
+                  pi0 = x0[u].y * c[u].x - x0[u].x * c[u].y;
+                  pr1 = x1[u].x * c[u].z + x1[u].y * c[u].w;
+                  pi1 = x1[u].y * c[u].z - x1[u].x * c[u].w;
+                } else {  // -(x * c)
+                  pr0 = -(x0[u].x * c[u].x - x0[u].y * c[u].y);
+                  pi0 = -(x0[u].x * c[u].y + x0[u].y * c[u].x);
+                  pr1 = -(x1[u].x * c[u].z - x1[u].y * c[u].w);
+                  pi1 = -(x1[u].x * c[u].w + x1[u].y * c[u].z);
+                }
+                kahan(ar, cr, pr0);
+                kahan(ai, ci, pi0);
+                kahan(ar, cr, pr1);
+                kahan(ai, ci, pi1);
+              }
             }
           }
         } else {
