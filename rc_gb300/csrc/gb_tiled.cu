@@ -76,12 +76,16 @@ struct __align__(16) GridRec {
   int32_t gcf;    // GCF element offset of the piece's first tap
   int32_t q0;     // accumulator index of the piece corner: yl * A + xl
   int32_t xm, ym; // piece corner mod P
-  int32_t wx, wy; // piece extent
   int32_t pitch;  // GCF row pitch (the plane's support S)
-  int32_t P;      // period of the run, | kWholePiece when the piece is P x P
+  int32_t shape;  // period P (bits 0-8), extents wx (9-17), wy (18-26), whole piece (bit 27)
+  float2 vis;     // the visibility
 };
+static_assert(sizeof(GridRec) == 32, "GridRec is two 16-byte words");
 
-constexpr int32_t kWholePiece = 1 << 16;
+constexpr int32_t kWholePiece = 1 << 27;
+__device__ __forceinline__ int shape_period(int32_t s) { return s & 0x1FF; }
+__device__ __forceinline__ int shape_wx(int32_t s) { return (s >> 9) & 0x1FF; }
+__device__ __forceinline__ int shape_wy(int32_t s) { return (s >> 18) & 0x1FF; }
 
 struct __align__(16) DegridRec {
   int32_t gcf, q0, pitch, vis;
@@ -105,10 +109,9 @@ __device__ __forceinline__ int slots_for(int P, int L) { return (P * P + L - 1) 
 template <int R, int U, bool FULL>
 __device__ __forceinline__ void grid_run(int k, int e, int lt, int L, int A,
                                          const GridRec* __restrict__ srec,
-                                         const float2* __restrict__ svis,
                                          float4* __restrict__ acc,
                                          const float2* __restrict__ gcf) {
-  const int P = srec[k].P & 0xFFFF;
+  const int P = shape_period(srec[k].shape);
   int ra[R], rb[R];
   bool own[R];  // slot m holds a residue (R L may exceed P^2)
 #pragma unroll
@@ -123,6 +126,43 @@ __device__ __forceinline__ void grid_run(int k, int e, int lt, int L, int A,
       rb[m] = kInvalidResidue;
     }
   }
+  if (FULL) {
+    // whole groups of U whole pieces: every owned slot has a tap, no tail checks
+    for (; k + U <= e; k += U) {
+      float2 c[U][R];
+      int qi[U][R];
+      float2 v[U];
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        const GridRec r = srec[k + u];
+        v[u] = r.vis;
+#pragma unroll
+        for (int m = 0; m < R; m++) {
+          int i = ra[m] - r.xm;
+          i += i < 0 ? P : 0;
+          int j = rb[m] - r.ym;
+          j += j < 0 ? P : 0;
+          c[u][m] = own[m] ? __ldg(gcf + r.gcf + j * r.pitch + i) : make_float2(0.f, 0.f);
+          qi[u][m] = r.q0 + j * A + i;
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+#pragma unroll
+        for (int m = 0; m < R; m++) {
+          if (own[m]) {
+            const int q = qi[u][m];
+            const float tr = v[u].x * c[u][m].x - v[u].y * c[u][m].y;
+            const float ti = v[u].x * c[u][m].y + v[u].y * c[u][m].x;
+            float4 s = acc[q];
+            kahan(s.x, s.z, tr);
+            kahan(s.y, s.w, ti);
+            acc[q] = s;
+          }
+        }
+      }
+    }
+  }
   for (; k < e; k += U) {
     float2 c[U][R];
     int qi[U][R];
@@ -131,14 +171,14 @@ __device__ __forceinline__ void grid_run(int k, int e, int lt, int L, int A,
     for (int u = 0; u < U; u++) {
       const bool live = k + u < e;
       const GridRec r = srec[live ? k + u : k];
-      v[u] = svis[live ? k + u : k];
+      v[u] = r.vis;
 #pragma unroll
       for (int m = 0; m < R; m++) {
         int i = ra[m] - r.xm;
         i += i < 0 ? P : 0;
         int j = rb[m] - r.ym;
         j += j < 0 ? P : 0;
-        if (live && own[m] && (FULL || (i < r.wx && j < r.wy))) {
+        if (live && own[m] && (FULL || (i < shape_wx(r.shape) && j < shape_wy(r.shape)))) {
           c[u][m] = __ldg(gcf + r.gcf + j * r.pitch + i);
           qi[u][m] = r.q0 + j * A + i;
         } else {
@@ -168,17 +208,16 @@ __device__ __forceinline__ void grid_run(int k, int e, int lt, int L, int A,
 template <bool FULL>
 __device__ __forceinline__ void grid_dispatch(int slots, int k, int e, int lt, int L, int A,
                                               const GridRec* __restrict__ srec,
-                                              const float2* __restrict__ svis,
                                               float4* __restrict__ acc,
                                               const float2* __restrict__ gcf) {
   switch (slots) {
-    case 1: grid_run<1, 8, FULL>(k, e, lt, L, A, srec, svis, acc, gcf); break;
-    case 2: grid_run<2, 4, FULL>(k, e, lt, L, A, srec, svis, acc, gcf); break;
-    case 3: grid_run<3, 3, FULL>(k, e, lt, L, A, srec, svis, acc, gcf); break;
-    case 4: grid_run<4, 2, FULL>(k, e, lt, L, A, srec, svis, acc, gcf); break;
+    case 1: grid_run<1, 8, FULL>(k, e, lt, L, A, srec, acc, gcf); break;
+    case 2: grid_run<2, 4, FULL>(k, e, lt, L, A, srec, acc, gcf); break;
+    case 3: grid_run<3, 3, FULL>(k, e, lt, L, A, srec, acc, gcf); break;
+    case 4: grid_run<4, 2, FULL>(k, e, lt, L, A, srec, acc, gcf); break;
     case 5:
-    case 6: grid_run<6, 1, FULL>(k, e, lt, L, A, srec, svis, acc, gcf); break;
-    default: grid_run<8, 1, FULL>(k, e, lt, L, A, srec, svis, acc, gcf); break;
+    case 6: grid_run<6, 1, FULL>(k, e, lt, L, A, srec, acc, gcf); break;
+    default: grid_run<8, 1, FULL>(k, e, lt, L, A, srec, acc, gcf); break;
   }
 }
 
@@ -186,7 +225,7 @@ __device__ __forceinline__ void grid_dispatch(int slots, int k, int e, int lt, i
 // (sum.re, sum.im, comp.re, comp.im) per pixel.
 __device__ __forceinline__ void grid_item(const TiledArgs& a, const Item& it, int lt, int L,
                                           int bar, bool whole, int A, float4* __restrict__ acc,
-                                          GridRec* __restrict__ srec, float2* __restrict__ svis,
+                                          GridRec* __restrict__ srec,
                                           const GridSlot& gs, const float2* __restrict__ gcf) {
   const float2* __restrict__ vis = gs.vis;
   float2* __restrict__ grid = gs.grid;
@@ -204,31 +243,44 @@ __device__ __forceinline__ void grid_item(const TiledArgs& a, const Item& it, in
       d.q0 = r.yl * A + r.xl;
       d.xm = r.xm;
       d.ym = r.ym;
-      d.wx = r.wx;
-      d.wy = r.wy;
       d.pitch = r.sm1 + 1;
-      d.P = (r.pm1 + 1) | (r.wx == r.pm1 + 1 && r.wy == r.pm1 + 1 ? kWholePiece : 0);
+      d.shape = (r.pm1 + 1) | (r.wx << 9) | (r.wy << 18) |
+                (r.wx == r.pm1 + 1 && r.wy == r.pm1 + 1 ? kWholePiece : 0);
+      d.vis = __ldg(vis + r.vis);
       srec[lt] = d;
-      svis[lt] = __ldg(vis + r.vis);
     }
     group_sync(bar, L, whole);
     int k = 0;
     while (k < nb) {
-      const int P = srec[k].P & 0xFFFF;
+      const int P = shape_period(srec[k].shape);
       if (P != curP) {
         // the residue map changes: finish every read-modify-write of the old one
         group_sync(bar, L, whole);
         curP = P;
       }
+      // the run's end, 32 records per step: records of an item are sorted by
+      // period, so the run ends at the first record of another period (every
+      // warp of the group reaches the same answer from the same records)
       int e = k;
       bool full = true;
-      for (; e < nb; e++) {
-        const int pe = srec[e].P;
-        if ((pe & 0xFFFF) != P) break;
-        full = full && (pe & kWholePiece);
+      const int lane = lt & 31;
+      for (;;) {
+        const int idx = e + lane;
+        const int pe = idx < nb ? srec[idx].shape : -1;
+        const bool stop = pe < 0 || shape_period(pe) != P;
+        const unsigned ms = __ballot_sync(0xFFFFFFFFu, stop);
+        const unsigned mp = __ballot_sync(0xFFFFFFFFu, !stop && !(pe & kWholePiece));
+        if (ms) {
+          const int first = __ffs(ms) - 1;
+          full = full && (mp & ((1u << first) - 1u)) == 0;
+          e += first;
+          break;
+        }
+        full = full && mp == 0;
+        e += 32;
       }
-      if (full) grid_dispatch<true>(slots_for(P, L), k, e, lt, L, A, srec, svis, acc, gcf);
-      else grid_dispatch<false>(slots_for(P, L), k, e, lt, L, A, srec, svis, acc, gcf);
+      if (full) grid_dispatch<true>(slots_for(P, L), k, e, lt, L, A, srec, acc, gcf);
+      else grid_dispatch<false>(slots_for(P, L), k, e, lt, L, A, srec, acc, gcf);
       k = e;
     }
   }
@@ -266,9 +318,8 @@ __global__ void __launch_bounds__(NT) k_grid_tiled(const __grid_constant__ Tiled
       unsigned char* base = smem + (size_t)g * grid_group_bytes(ci.A, ci.L);
       float4* acc = (float4*)base;
       GridRec* srec = (GridRec*)(base + 16 * (size_t)AA);
-      float2* svis = (float2*)(base + 16 * (size_t)AA + 32 * (size_t)ci.L);
       grid_item(a, a.items[bd.first_item + g], lt, ci.L, 1 + g, ci.L == NT, ci.A, acc, srec,
-                svis, gp.s[bd.grid], gcf);
+                gp.s[bd.grid], gcf);
     }
     __syncthreads();
   }
