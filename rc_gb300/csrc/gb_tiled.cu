@@ -286,13 +286,21 @@ __device__ __forceinline__ void grid_item(const TiledArgs& a, const Item& it, in
   }
   group_sync(bar, L, whole);
   const int x0 = it.tile_x * a.T, y0 = it.tile_y * a.T;
+  // pixel q = lt + n L walks (py, px) by L / A rows and L mod A columns
+  const int dy = L / A, dx = L - dy * A;
+  int py = lt / A, px = lt - py * A;
   for (int q = lt; q < AA; q += L) {
     const float4 s = acc[q];
     if (s.x != 0.f || s.y != 0.f || s.z != 0.f || s.w != 0.f) {
-      const int py = q / A, px = q - py * A;
       const int gx = x0 + px, gy = y0 + py;
       if (gx < gs.ext_x && gy < gs.ext_y)
         atomicAdd(grid + (int64_t)gy * gs.pitch + gx, make_float2(s.x - s.z, s.y - s.w));
+    }
+    px += dx;
+    py += dy;
+    if (px >= A) {
+      px -= A;
+      py++;
     }
   }
 }
@@ -340,9 +348,16 @@ __device__ __forceinline__ void degrid_item(const TiledArgs& a, const Item& it, 
   const int x0 = it.tile_x * a.T, y0 = it.tile_y * a.T;
   // asynchronous copies straight into shared memory (no register round
   // trip), all in flight at once; pixels outside the grid are zero-filled
+  const int dy = L / A, dx = L - dy * A;  // q = lt + n L walks (py, px) without divisions
+  int py = lt / A, px = lt - py * A;
   for (int q = lt; q < AA; q += L) {
-    const int py = q / A, px = q - py * A;
     const int gx = x0 + px, gy = y0 + py;
+    px += dx;
+    py += dy;
+    if (px >= A) {
+      px -= A;
+      py++;
+    }
     const bool in = gx < gs.ext_x && gy < gs.ext_y;
     const float2* src = in ? grid + (int64_t)gy * gs.pitch + gx : grid;
     const unsigned dst = (unsigned)__cvta_generic_to_shared(sg + q);
