@@ -74,7 +74,7 @@ __device__ __forceinline__ ClassInfo class_of(const TiledArgs& a, int c) {
 // threads of a group read plain ints instead of unpacking bytes per tap.
 struct __align__(16) GridRec {
   int32_t gcf;    // GCF element offset of the piece's first tap
-  int32_t q0;     // accumulator index of the piece corner: yl * A + xl
+  int32_t q0;     // accumulator index of the piece corner: yl * acc_stride(A) + xl
   int32_t xm, ym; // piece corner mod P
   int32_t pitch;  // GCF row pitch (the plane's support S)
   int32_t shape;  // period P (bits 0-8), extents wx (9-17), wy (18-26), whole piece (bit 27)
@@ -107,7 +107,7 @@ __device__ __forceinline__ int slots_for(int P, int L) { return (P * P + L - 1) 
 // FULL: every piece of the run is a whole P x P square, so every owned
 // residue has a tap and the extent checks drop out.
 template <int R, int U, bool FULL>
-__device__ __forceinline__ void grid_run(int k, int e, int lt, int L, int A,
+__device__ __forceinline__ void grid_run(int k, int e, int lt, int L, int As,
                                          const GridRec* __restrict__ srec,
                                          float4* __restrict__ acc,
                                          const float2* __restrict__ gcf) {
@@ -143,7 +143,7 @@ __device__ __forceinline__ void grid_run(int k, int e, int lt, int L, int A,
           int j = rb[m] - r.ym;
           j += j < 0 ? P : 0;
           c[u][m] = own[m] ? __ldg(gcf + r.gcf + j * r.pitch + i) : make_float2(0.f, 0.f);
-          qi[u][m] = r.q0 + j * A + i;
+          qi[u][m] = r.q0 + j * As + i;
         }
       }
 #pragma unroll
@@ -180,7 +180,7 @@ __device__ __forceinline__ void grid_run(int k, int e, int lt, int L, int A,
         j += j < 0 ? P : 0;
         if (live && own[m] && (FULL || (i < shape_wx(r.shape) && j < shape_wy(r.shape)))) {
           c[u][m] = __ldg(gcf + r.gcf + j * r.pitch + i);
-          qi[u][m] = r.q0 + j * A + i;
+          qi[u][m] = r.q0 + j * As + i;
         } else {
           c[u][m] = make_float2(0.f, 0.f);
           qi[u][m] = -1;
@@ -206,18 +206,18 @@ __device__ __forceinline__ void grid_run(int k, int e, int lt, int L, int A,
 }
 
 template <bool FULL>
-__device__ __forceinline__ void grid_dispatch(int slots, int k, int e, int lt, int L, int A,
+__device__ __forceinline__ void grid_dispatch(int slots, int k, int e, int lt, int L, int As,
                                               const GridRec* __restrict__ srec,
                                               float4* __restrict__ acc,
                                               const float2* __restrict__ gcf) {
   switch (slots) {
-    case 1: grid_run<1, 8, FULL>(k, e, lt, L, A, srec, acc, gcf); break;
-    case 2: grid_run<2, 4, FULL>(k, e, lt, L, A, srec, acc, gcf); break;
-    case 3: grid_run<3, 3, FULL>(k, e, lt, L, A, srec, acc, gcf); break;
-    case 4: grid_run<4, 2, FULL>(k, e, lt, L, A, srec, acc, gcf); break;
+    case 1: grid_run<1, 8, FULL>(k, e, lt, L, As, srec, acc, gcf); break;
+    case 2: grid_run<2, 4, FULL>(k, e, lt, L, As, srec, acc, gcf); break;
+    case 3: grid_run<3, 3, FULL>(k, e, lt, L, As, srec, acc, gcf); break;
+    case 4: grid_run<4, 2, FULL>(k, e, lt, L, As, srec, acc, gcf); break;
     case 5:
-    case 6: grid_run<6, 1, FULL>(k, e, lt, L, A, srec, acc, gcf); break;
-    default: grid_run<8, 1, FULL>(k, e, lt, L, A, srec, acc, gcf); break;
+    case 6: grid_run<6, 1, FULL>(k, e, lt, L, As, srec, acc, gcf); break;
+    default: grid_run<8, 1, FULL>(k, e, lt, L, As, srec, acc, gcf); break;
   }
 }
 
@@ -229,7 +229,7 @@ __device__ __forceinline__ void grid_item(const TiledArgs& a, const Item& it, in
                                           const GridSlot& gs, const float2* __restrict__ gcf) {
   const float2* __restrict__ vis = gs.vis;
   float2* __restrict__ grid = gs.grid;
-  const int AA = A * A;
+  const int As = acc_stride(A), AA = A * As;
   for (int q = lt; q < AA; q += L) acc[q] = make_float4(0.f, 0.f, 0.f, 0.f);
   int curP = -1;
   const int end = it.start + it.count;
@@ -240,7 +240,7 @@ __device__ __forceinline__ void grid_item(const TiledArgs& a, const Item& it, in
       const Rec r = a.recs[base + lt];
       GridRec d;
       d.gcf = (int32_t)r.gcf;
-      d.q0 = r.yl * A + r.xl;
+      d.q0 = r.yl * As + r.xl;
       d.xm = r.xm;
       d.ym = r.ym;
       d.pitch = r.sm1 + 1;
@@ -279,27 +279,28 @@ __device__ __forceinline__ void grid_item(const TiledArgs& a, const Item& it, in
         full = full && mp == 0;
         e += 32;
       }
-      if (full) grid_dispatch<true>(slots_for(P, L), k, e, lt, L, A, srec, acc, gcf);
-      else grid_dispatch<false>(slots_for(P, L), k, e, lt, L, A, srec, acc, gcf);
+      if (full) grid_dispatch<true>(slots_for(P, L), k, e, lt, L, As, srec, acc, gcf);
+      else grid_dispatch<false>(slots_for(P, L), k, e, lt, L, As, srec, acc, gcf);
       k = e;
     }
   }
   group_sync(bar, L, whole);
   const int x0 = it.tile_x * a.T, y0 = it.tile_y * a.T;
-  // pixel q = lt + n L walks (py, px) by L / A rows and L mod A columns
-  const int dy = L / A, dx = L - dy * A;
-  int py = lt / A, px = lt - py * A;
+  // pixel q = lt + n L walks (py, px) by L / As rows and L mod As columns;
+  // the padding columns px >= A are never touched
+  const int dy = L / As, dx = L - dy * As;
+  int py = lt / As, px = lt - py * As;
   for (int q = lt; q < AA; q += L) {
     const float4 s = acc[q];
-    if (s.x != 0.f || s.y != 0.f || s.z != 0.f || s.w != 0.f) {
+    if (px < A && (s.x != 0.f || s.y != 0.f || s.z != 0.f || s.w != 0.f)) {
       const int gx = x0 + px, gy = y0 + py;
       if (gx < gs.ext_x && gy < gs.ext_y)
         atomicAdd(grid + (int64_t)gy * gs.pitch + gx, make_float2(s.x - s.z, s.y - s.w));
     }
     px += dx;
     py += dy;
-    if (px >= A) {
-      px -= A;
+    if (px >= As) {
+      px -= As;
       py++;
     }
   }
@@ -322,10 +323,9 @@ __global__ void __launch_bounds__(NT) k_grid_tiled(const __grid_constant__ Tiled
     const int g = tid / ci.L;
     if (g < bd.n_items) {
       const int lt = tid - g * ci.L;
-      const int AA = ci.A * ci.A;
       unsigned char* base = smem + (size_t)g * grid_group_bytes(ci.A, ci.L);
       float4* acc = (float4*)base;
-      GridRec* srec = (GridRec*)(base + 16 * (size_t)AA);
+      GridRec* srec = (GridRec*)(base + 16 * (size_t)ci.A * acc_stride(ci.A));
       grid_item(a, a.items[bd.first_item + g], lt, ci.L, 1 + g, ci.L == NT, ci.A, acc, srec,
                 gp.s[bd.grid], gcf);
     }
