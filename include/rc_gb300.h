@@ -153,6 +153,15 @@ int gb_plan_destroy(gb_plan *plan);
  * [5] largest support, [6] threads per CTA. */
 int gb_plan_stats(const gb_plan *plan, int64_t *stats7);
 
+/* Device-side status of a plan's degridding, read synchronously on `stream`:
+ * out2[0] = 1 when a TMA stage of a degridding launch did not complete within
+ * its bounded wait since the last call (that launch's predictions are then
+ * invalid; the word is cleared by this call), out2[1] = 1 when the last
+ * degridding launch staged its grid regions with TMA (single grid, even tile
+ * edge, even row pitch, 16-byte aligned grid), 0 when it used per-thread
+ * asynchronous copies.  Returns GB_ERR_TIMEOUT when out2[0] is set. */
+int gb_plan_device_status(gb_plan *plan, int32_t *out2, void *stream);
+
 /* Per-visibility index record (x0, y0, phase ou+8*ov, plane, kept) as the
  * plan computed it, 5 int32 per visibility, into device memory. */
 int gb_plan_export_index(const gb_plan *plan, int32_t *d_out5, void *stream);

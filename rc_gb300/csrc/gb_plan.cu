@@ -273,12 +273,16 @@ static int build_plan(gb_plan* P, const gb_geometry* geo, int64_t n_vis, const d
   P->smem_degrid = tiled_smem_degrid(P->cls, P->n_classes, P->NT);
   P->ctas_per_sm_grid = tiled_ctas_per_sm(P, true);
   P->ctas_per_sm_degrid = tiled_ctas_per_sm(P, false);
+  P->ctas_per_sm_degrid_tma = tiled_ctas_per_sm(P, false, true);
 
   // ---- device tables
   if ((rc = dalloc(&P->d_plane, n_vis)) || (rc = dalloc(&P->d_supports, np)) ||
       (rc = dalloc(&P->d_offsets, np)) || (rc = dalloc(&P->d_planes, np)) ||
-      (rc = dalloc(&P->d_queue, 2)))
+      (rc = dalloc(&P->d_queue, 3)))
     return rc;
+  // [0], [1]: work-queue heads of the grid and degrid kernels; [2]: device
+  // error word (a TMA stage completion not seen in time)
+  GB_CUDA_TRY(cudaMemsetAsync(P->d_queue, 0, 3 * sizeof(int32_t), s));
   GB_CUDA_TRY(cudaMemcpyAsync(P->d_supports, geo->supports, sizeof(int32_t) * np,
                               cudaMemcpyHostToDevice, s));
   GB_CUDA_TRY(cudaMemcpyAsync(P->d_offsets, geo->gcf_offsets, sizeof(int64_t) * np,
@@ -534,6 +538,25 @@ extern "C" int gb_plan_stats(const gb_plan* P, int64_t* st) {
   st[4] = P->T;
   st[5] = P->max_support;
   st[6] = P->NT;
+  return GB_OK;
+}
+
+extern "C" int gb_plan_device_status(gb_plan* P, int32_t* out2, void* stream) {
+  if (!P || !out2) {
+    gb_set_error(GB_ERR_ARG, "gb_plan_device_status: NULL argument");
+    return GB_ERR_ARG;
+  }
+  int32_t err = 0;
+  cudaStream_t s = (cudaStream_t)stream;
+  GB_CUDA_TRY(cudaMemcpyAsync(&err, P->d_queue + 2, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  GB_CUDA_TRY(cudaMemsetAsync(P->d_queue + 2, 0, sizeof(int32_t), s));
+  GB_CUDA_TRY(cudaStreamSynchronize(s));
+  out2[0] = err;
+  out2[1] = P->last_stage_tma;
+  if (err) {
+    gb_set_error(GB_ERR_TIMEOUT, "degridding: a TMA stage did not complete in time");
+    return GB_ERR_TIMEOUT;
+  }
   return GB_OK;
 }
 

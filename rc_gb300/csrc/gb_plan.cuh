@@ -15,6 +15,7 @@
 // accumulator stays within shared memory whatever the support.
 #pragma once
 
+#include <cuda.h>
 #include <stdint.h>
 
 #include <vector>
@@ -85,8 +86,12 @@ __host__ __device__ inline size_t grid_group_bytes(int A, int L) {
 }
 // The float2 grid stage is padded to 16 bytes so that the 16-byte records
 // behind it (and the next group's region) stay 16-byte aligned.
+// Degridding stages the A x A grid region with rows padded to an even width
+// (a TMA box row must be a multiple of 16 bytes) and starts each group's
+// region on a 128-byte boundary (TMA destination).
+__host__ __device__ inline int stage_stride(int A) { return (A + 1) & ~1; }
 __host__ __device__ inline size_t degrid_stage_bytes(int A) {
-  return (8 * (size_t)A * A + 15) & ~(size_t)15;
+  return (8 * (size_t)A * stage_stride(A) + 127) & ~(size_t)127;
 }
 __host__ __device__ inline size_t degrid_group_bytes(int A, int L) {
   return degrid_stage_bytes(A) + 32 * (size_t)L;
@@ -131,7 +136,7 @@ struct gb_plan {
   int n_classes = 0;
   gb::ClassInfo cls[gb::kMaxClasses] = {};
   size_t smem_grid = 0, smem_degrid = 0;
-  int ctas_per_sm_grid = 1, ctas_per_sm_degrid = 1;
+  int ctas_per_sm_grid = 1, ctas_per_sm_degrid = 1, ctas_per_sm_degrid_tma = 1;
   // device arrays owned by the plan
   int32_t* d_plane = nullptr;
   int32_t* d_supports = nullptr;
@@ -146,6 +151,14 @@ struct gb_plan {
   int64_t kept = 0, taps = 0, tiles_used = 0;
   bool own_plane = true;
   std::vector<gb::HostItem> host_items;  // in d_items order (grid slot 0)
+  // TMA descriptors of the last degridded grid, one per thread-group class
+  // (box = that class's stage); rebuilt when the grid's address or shape changes
+  const void* tma_grid = nullptr;
+  int tma_ext_x = 0, tma_ext_y = 0;
+  int64_t tma_pitch = 0;
+  bool tma_ok = false;
+  CUtensorMap tma_maps[gb::kMaxClasses];
+  int last_stage_tma = 0;  // 1: the last degridding launch staged with TMA
 };
 
 namespace gb {
@@ -176,5 +189,5 @@ int launch_tiled_batch(bool grid_mode, int mode, int NT, size_t smem, int ctas_p
                        const GridPtrs& gp, const float* gcf, cudaStream_t s);
 int tiled_ctas_per_sm_for(int NT, bool grid, size_t smem);
 // Resident CTAs per SM of the tiled grid (or degrid) kernel for this plan.
-int tiled_ctas_per_sm(const gb_plan* plan, bool grid);
+int tiled_ctas_per_sm(const gb_plan* plan, bool grid, bool tma = false);
 }  // namespace gb

@@ -310,7 +310,7 @@ template <int NT>
 __global__ void __launch_bounds__(NT) k_grid_tiled(const __grid_constant__ TiledArgs a,
                                                    const __grid_constant__ GridPtrs gp,
                                                    const float2* __restrict__ gcf) {
-  extern __shared__ __align__(16) unsigned char smem[];
+  extern __shared__ __align__(128) unsigned char smem[];
   __shared__ int s_b;
   const int tid = threadIdx.x;
   for (;;) {
@@ -333,39 +333,117 @@ __global__ void __launch_bounds__(NT) k_grid_tiled(const __grid_constant__ Tiled
   }
 }
 
+// ------------------------------------------------------------ TMA staging
+// Degridding stages each item's grid region either with one 2-D bulk tensor
+// copy (TMA) issued by the group's first thread and completing on an
+// mbarrier (k_degrid_tiled<.., true>), or, where no tensor map applies
+// (several grids in one launch, odd tile edge, unaligned grid), with
+// asynchronous per-thread copies (k_degrid_tiled<.., false>).
+struct StageMaps {
+  CUtensorMap m[kMaxClasses];  // per thread-group class: box = that class's stage
+  int32_t* err;                // set when a TMA completion is not seen in time
+};
+
+// One mbarrier per group slot of a CTA (groups have >= 64 threads, CTAs at
+// most 512) and the parity each slot's barrier completes next (bit per slot).
+constexpr int kMaxGroupSlots = 8;
+__shared__ __align__(8) uint64_t g_stage_bar[kMaxGroupSlots];
+__shared__ unsigned g_stage_phase;
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) {
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
+               : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
+  asm volatile(
+      "{\n .reg .b64 st;\n mbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n}" ::"r"(
+          smem_u32(bar)),
+      "r"(bytes)
+      : "memory");
+}
+
+// Bounded wait for the phase with the given parity: each try suspends for at
+// most about a microsecond, and about half a million tries give up.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
+  const unsigned a = smem_u32(bar);
+  for (int n = 0; n < (1 << 19); n++) {
+    unsigned done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n"
+        " selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(done)
+        : "r"(a), "r"(parity), "r"(1000u)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+// Box at element (x, y) of the tensor map into shared memory; x * 8 bytes is a
+// multiple of 16 (even tile edge), y is any row.
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar,
+                                            int x, int y) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3}], [%4];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ const CUtensorMap* stage_map(const StageMaps& sm, int c) {
+  static_assert(kMaxClasses == 4, "stage_map covers 4 classes");
+  return c == 0 ? &sm.m[0] : c == 1 ? &sm.m[1] : c == 2 ? &sm.m[2] : &sm.m[3];
+}
+
 // Degridding of one item: stage the A x A grid region, then batches of L
 // decoded records; sub-warps of SW lanes take one piece each (32/SW pieces
 // per warp at a time), lanes stride the piece's taps by SW, Kahan per lane,
 // shuffle reduction within the sub-warp.
-template <int MODE, int SW>
+template <int MODE, int SW, bool TMA>
 __device__ __forceinline__ void degrid_item(const TiledArgs& a, const Item& it, int lt, int L,
                                             int bar, bool whole, int A, float2* __restrict__ sg,
                                             DegridRec* __restrict__ srec, const GridSlot& gs,
-                                            const float2* __restrict__ gcf) {
+                                            const float2* __restrict__ gcf,
+                                            const StageMaps& sm, int cls, int slot) {
   const float2* __restrict__ grid = gs.grid;
   float2* __restrict__ pred = gs.vis;
-  const int AA = A * A;
+  const int Ae = stage_stride(A);  // stage row stride (even)
   const int x0 = it.tile_x * a.T, y0 = it.tile_y * a.T;
-  // asynchronous copies straight into shared memory (no register round
-  // trip), all in flight at once; pixels outside the grid are zero-filled
-  const int dy = L / A, dx = L - dy * A;  // q = lt + n L walks (py, px) without divisions
-  int py = lt / A, px = lt - py * A;
-  for (int q = lt; q < AA; q += L) {
-    const int gx = x0 + px, gy = y0 + py;
-    px += dx;
-    py += dy;
-    if (px >= A) {
-      px -= A;
-      py++;
+  if constexpr (TMA) {
+    if (lt == 0) {
+      // the stage's earlier reads (generic proxy) come before the copy's writes
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      mbar_expect_tx(&g_stage_bar[slot], (unsigned)(A * Ae * 8));
+      tma_load_2d(sg, stage_map(sm, cls), &g_stage_bar[slot], x0, y0);
     }
-    const bool in = gx < gs.ext_x && gy < gs.ext_y;
-    const float2* src = in ? grid + (int64_t)gy * gs.pitch + gx : grid;
-    const unsigned dst = (unsigned)__cvta_generic_to_shared(sg + q);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(dst), "l"(src),
-                 "r"(in ? 8 : 0)
-                 : "memory");
+  } else {
+    // asynchronous copies straight into shared memory (no register round
+    // trip), all in flight at once; pixels outside the grid are zero-filled
+    const int AA = A * Ae;
+    const int dy = L / Ae, dx = L - dy * Ae;  // q = lt + n L walks (py, px) without divisions
+    int py = lt / Ae, px = lt - py * Ae;
+    for (int q = lt; q < AA; q += L) {
+      const int gx = x0 + px, gy = y0 + py;
+      const bool in = px < A && gx < gs.ext_x && gy < gs.ext_y;
+      px += dx;
+      py += dy;
+      if (px >= Ae) {
+        px -= Ae;
+        py++;
+      }
+      const float2* src = in ? grid + (int64_t)gy * gs.pitch + gx : grid;
+      const unsigned dst = (unsigned)__cvta_generic_to_shared(sg + q);
+      asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(dst), "l"(src),
+                   "r"(in ? 8 : 0)
+                   : "memory");
+    }
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
   }
-  asm volatile("cp.async.commit_group;\n" ::: "memory");
   constexpr int SUBS = 32 / SW;
   const bool gcf16 = (reinterpret_cast<uintptr_t>(gcf) & 15) == 0;
   const int nw = L >> 5, w = lt >> 5, lane = lt & 31;
@@ -378,7 +456,7 @@ __device__ __forceinline__ void degrid_item(const TiledArgs& a, const Item& it, 
       const Rec r = a.recs[base + lt];
       DegridRec d;
       d.gcf = (int32_t)r.gcf;
-      d.q0 = r.yl * A + r.xl;
+      d.q0 = r.yl * Ae + r.xl;
       d.pitch = r.sm1 + 1;
       d.vis = r.vis;
       d.wx = r.wx;
@@ -393,10 +471,23 @@ __device__ __forceinline__ void degrid_item(const TiledArgs& a, const Item& it, 
       d.flags = (r.sm1 > r.pm1 ? kRecCut : 0) | (paired ? kRecPaired : 0);
       srec[lt] = d;
     }
-    // this thread's staging copies (issued before the first batch's record
-    // loads, so the two latencies overlap); the barrier publishes them all
-    if (base == it.start) asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+    // the stage (issued before the first batch's record loads, so the two
+    // latencies overlap); the barrier publishes per-thread copies to the group
+    if (base == it.start) {
+      if constexpr (TMA) {
+        const unsigned parity = (*(volatile unsigned*)&g_stage_phase >> slot) & 1u;
+        // once any wait has run out, later items do not wait again
+        if (*(volatile int32_t*)sm.err == 0 && !mbar_wait(&g_stage_bar[slot], parity))
+          atomicOr(sm.err, 1);
+      } else {
+        asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+      }
+    }
     group_sync(bar, L, whole);
+    // every thread of the group has read the phase: the next use of this
+    // slot's barrier waits for the other parity
+    if constexpr (TMA)
+      if (base == it.start && lt == 0) atomicXor(&g_stage_phase, 1u << slot);
     for (int kk = w * SUBS; kk < nb; kk += nw * SUBS) {
       const int k = kk + sub;
       const bool live = k < nb;
@@ -422,7 +513,7 @@ __device__ __forceinline__ void degrid_item(const TiledArgs& a, const Item& it, 
 #pragma unroll
             for (int u = 0; u < UN; u++) {
               off_g[u] = j * p2 + i;
-              off_s[u] = j * A + 2 * i;
+              off_s[u] = j * Ae + 2 * i;
               i += di;
               j += dj;
               if (i >= w2) {
@@ -468,7 +559,7 @@ __device__ __forceinline__ void degrid_item(const TiledArgs& a, const Item& it, 
 #pragma unroll 4
           for (; j < r.wy;) {
             const float2 c = __ldg(gp + j * r.pitch + i);
-            const float2 x = sp[j * A + i];
+            const float2 x = sp[j * Ae + i];
             float pr, pi;
             if (MODE == 0) {  // x * conj(c)
               pr = x.x * c.x + x.y * c.y;
@@ -505,13 +596,22 @@ __device__ __forceinline__ void degrid_item(const TiledArgs& a, const Item& it, 
   }
 }
 
-template <int NT, int MODE>
-__global__ void __launch_bounds__(NT) k_degrid_tiled(const __grid_constant__ TiledArgs a,
-                                                     const __grid_constant__ GridPtrs gp,
-                                                     const float2* __restrict__ gcf) {
-  extern __shared__ __align__(16) unsigned char smem[];
+// At most 64 registers per thread (1024 resident threads per SM): registers
+// then do not cut the CTAs per SM below what shared memory allows.
+template <int NT, int MODE, bool TMA>
+__global__ void __launch_bounds__(NT, 1024 / NT)
+    k_degrid_tiled(const __grid_constant__ TiledArgs a, const __grid_constant__ GridPtrs gp,
+                   const __grid_constant__ StageMaps sm, const float2* __restrict__ gcf) {
+  static_assert(NT / 64 <= kMaxGroupSlots, "one stage barrier per group slot");
+  extern __shared__ __align__(128) unsigned char smem[];
   __shared__ int s_b;
   const int tid = threadIdx.x;
+  if constexpr (TMA) {
+    if (tid < NT / 64) mbar_init(&g_stage_bar[tid], 1);
+    if (tid == 0) g_stage_phase = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    __syncthreads();
+  }
   for (;;) {
     if (tid == 0) s_b = atomicAdd(a.queue + 1, 1);
     __syncthreads();
@@ -529,11 +629,14 @@ __global__ void __launch_bounds__(NT) k_degrid_tiled(const __grid_constant__ Til
       const bool whole = ci.L == NT;
       // sub-warp width by piece size: <= 64 taps -> 8 lanes, <= 256 -> 16, else 32
       if (ci.pmax <= 8)
-        degrid_item<MODE, 8>(a, it, lt, ci.L, 1 + g, whole, ci.A, sg, srec, gp.s[bd.grid], gcf);
+        degrid_item<MODE, 8, TMA>(a, it, lt, ci.L, 1 + g, whole, ci.A, sg, srec,
+                                   gp.s[bd.grid], gcf, sm, bd.cls, g);
       else if (ci.pmax <= 16)
-        degrid_item<MODE, 16>(a, it, lt, ci.L, 1 + g, whole, ci.A, sg, srec, gp.s[bd.grid], gcf);
+        degrid_item<MODE, 16, TMA>(a, it, lt, ci.L, 1 + g, whole, ci.A, sg, srec,
+                                   gp.s[bd.grid], gcf, sm, bd.cls, g);
       else
-        degrid_item<MODE, 32>(a, it, lt, ci.L, 1 + g, whole, ci.A, sg, srec, gp.s[bd.grid], gcf);
+        degrid_item<MODE, 32, TMA>(a, it, lt, ci.L, 1 + g, whole, ci.A, sg, srec,
+                                   gp.s[bd.grid], gcf, sm, bd.cls, g);
     }
     __syncthreads();
   }
@@ -566,16 +669,21 @@ int tiled_max_smem() {
 }
 
 typedef void (*GridFn)(const TiledArgs, const GridPtrs, const float2*);
-typedef void (*DegridFn)(const TiledArgs, const GridPtrs, const float2*);
+typedef void (*DegridFn)(const TiledArgs, const GridPtrs, const StageMaps, const float2*);
 
 static GridFn grid_fn(int NT) {
   return NT == 128 ? k_grid_tiled<128> : NT == 256 ? k_grid_tiled<256> : k_grid_tiled<512>;
 }
 
-static DegridFn degrid_fn(int NT, int mode) {
-  if (NT == 128) return mode ? k_degrid_tiled<128, 1> : k_degrid_tiled<128, 0>;
-  if (NT == 256) return mode ? k_degrid_tiled<256, 1> : k_degrid_tiled<256, 0>;
-  return mode ? k_degrid_tiled<512, 1> : k_degrid_tiled<512, 0>;
+template <bool TMA>
+static DegridFn degrid_fn_t(int NT, int mode) {
+  if (NT == 128) return mode ? k_degrid_tiled<128, 1, TMA> : k_degrid_tiled<128, 0, TMA>;
+  if (NT == 256) return mode ? k_degrid_tiled<256, 1, TMA> : k_degrid_tiled<256, 0, TMA>;
+  return mode ? k_degrid_tiled<512, 1, TMA> : k_degrid_tiled<512, 0, TMA>;
+}
+
+static DegridFn degrid_fn(int NT, int mode, bool tma = false) {
+  return tma ? degrid_fn_t<true>(NT, mode) : degrid_fn_t<false>(NT, mode);
 }
 
 static int set_smem_attr(const void* fn) {
@@ -584,11 +692,11 @@ static int set_smem_attr(const void* fn) {
   return GB_OK;
 }
 
-int tiled_ctas_per_sm(const gb_plan* P, bool grid) {
+int tiled_ctas_per_sm(const gb_plan* P, bool grid, bool tma) {
   const void* fn = grid ? (const void*)grid_fn(P->NT)
-                        : (const void*)degrid_fn(P->NT, 0);
+                        : (const void*)degrid_fn(P->NT, 0, tma);
   if (set_smem_attr(fn)) return 1;
-  if (!grid) set_smem_attr((const void*)degrid_fn(P->NT, 1));
+  if (!grid) set_smem_attr((const void*)degrid_fn(P->NT, 1, tma));
   int n = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, P->NT,
                                                 grid ? P->smem_grid : P->smem_degrid);
@@ -632,15 +740,83 @@ int launch_grid_tiled(gb_plan* P, const float* vis, const float* gcf, float* gri
   return GB_OK;
 }
 
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// against the driver library).
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                  const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                  const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_tiled() {
+  static EncodeTiledFn fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (EncodeTiledFn)p;
+  });
+  return fn;
+}
+
+// Tensor maps of the grid for TMA staging, one per class (box = Ae x A
+// pixels of 8 bytes, rows of pitch * 8 bytes, zero fill outside ext_x x
+// ext_y), cached on the plan.  False where TMA does not apply: an odd tile
+// edge (the box's x would not start on 16 bytes), an odd pitch, an unaligned
+// grid, an oversized box or no encoder; degridding then stages with
+// per-thread copies.
+static bool stage_maps(gb_plan* P, const float* grid, StageMaps* out) {
+  const int64_t pitch = P->dev.pitch;
+  const int ex = P->dev.ext_x, ey = P->dev.ext_y;
+  if ((P->T & 1) || (pitch & 1) || (reinterpret_cast<uintptr_t>(grid) & 15) || ex <= 0 ||
+      ey <= 0 || P->NT / 64 > kMaxGroupSlots)
+    return false;
+  for (int c = 0; c < P->n_classes; c++)
+    if (P->cls[c].A > 256 || stage_stride(P->cls[c].A) > 256 || P->cls[c].L < 64) return false;
+  if (!(P->tma_ok && P->tma_grid == grid && P->tma_ext_x == ex && P->tma_ext_y == ey &&
+        P->tma_pitch == pitch)) {
+    P->tma_ok = false;
+    EncodeTiledFn enc = encode_tiled();
+    if (!enc) return false;
+    for (int c = 0; c < P->n_classes; c++) {
+      const int A = P->cls[c].A;
+      const cuuint64_t dims[2] = {(cuuint64_t)ex, (cuuint64_t)ey};
+      const cuuint64_t strides[1] = {(cuuint64_t)pitch * 8};
+      const cuuint32_t box[2] = {(cuuint32_t)stage_stride(A), (cuuint32_t)A};
+      const cuuint32_t estr[2] = {1, 1};
+      if (enc(&P->tma_maps[c], CU_TENSOR_MAP_DATA_TYPE_UINT64, 2, (void*)grid, dims, strides,
+              box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+              CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return false;
+    }
+    P->tma_grid = grid;
+    P->tma_ext_x = ex;
+    P->tma_ext_y = ey;
+    P->tma_pitch = pitch;
+    P->tma_ok = true;
+  }
+  for (int c = 0; c < P->n_classes; c++) out->m[c] = P->tma_maps[c];
+  return true;
+}
+
 int launch_degrid_tiled(gb_plan* P, const float* gcf, const float* grid, float* pred, int mode,
                         cudaStream_t s) {
   GB_CUDA_TRY(cudaMemsetAsync(pred, 0, sizeof(float2) * (size_t)P->dev.n_vis, s));
   if (P->n_bundles == 0) return GB_OK;
   GB_CUDA_TRY(cudaMemsetAsync(P->d_queue + 1, 0, sizeof(int32_t), s));
-  const int blocks = std::min(P->n_bundles, sm_count() * P->ctas_per_sm_degrid);
-  DegridFn fn = degrid_fn(P->NT, mode);
+  StageMaps sm;
+  memset(&sm, 0, sizeof(sm));
+  const bool tma = stage_maps(P, grid, &sm);
+  sm.err = P->d_queue + 2;
+  P->last_stage_tma = tma ? 1 : 0;
+  const int per_sm = tma ? P->ctas_per_sm_degrid_tma : P->ctas_per_sm_degrid;
+  const int blocks = std::min(P->n_bundles, sm_count() * per_sm);
+  DegridFn fn = degrid_fn(P->NT, mode, tma);
   fn<<<blocks, P->NT, P->smem_degrid, s>>>(
-      make_args(P), one_grid(grid, pred, P->dev.ext_x, P->dev.ext_y, P->dev.pitch),
+      make_args(P), one_grid(grid, pred, P->dev.ext_x, P->dev.ext_y, P->dev.pitch), sm,
       (const float2*)gcf);
   GB_CUDA_TRY(cudaGetLastError());
   return GB_OK;
@@ -695,8 +871,10 @@ int launch_tiled_batch(bool grid_mode, int mode, int NT, size_t smem, int ctas_p
     GridFn fn = grid_fn(NT);
     fn<<<blocks, NT, smem, s>>>(a, gp, (const float2*)gcf);
   } else {
+    StageMaps sm;  // several grids: per-thread asynchronous staging
+    memset(&sm, 0, sizeof(sm));
     DegridFn fn = degrid_fn(NT, mode);
-    fn<<<blocks, NT, smem, s>>>(a, gp, (const float2*)gcf);
+    fn<<<blocks, NT, smem, s>>>(a, gp, sm, (const float2*)gcf);
   }
   GB_CUDA_TRY(cudaGetLastError());
   return GB_OK;

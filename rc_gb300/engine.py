@@ -77,6 +77,15 @@ class Plan:
         keys = ["kept", "taps", "items", "tiles", "tile", "max_support", "threads"]
         return dict(zip(keys, list(st)))
 
+    def device_status(self, stream=None):
+        """(error, staged_with_tma) of the last degridding launches: error = 1
+        when a TMA stage did not complete in time (cleared by this call)."""
+        out = (C.c_int32 * 2)()
+        rc = self.L.gb_plan_device_status(self.h, out, _stream(stream))
+        if rc not in (_lib.GB_OK, _lib.ERR_TIMEOUT):
+            _lib.check(rc, "gb_plan_device_status")
+        return int(out[0]), int(out[1])
+
     def export_index(self, stream=None):
         import torch
 

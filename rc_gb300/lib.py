@@ -127,6 +127,7 @@ SIGNATURES = {
                                  C.POINTER(_VP)]),
     "gb_plan_destroy": (C.c_int, [_VP]),
     "gb_plan_stats": (C.c_int, [_VP, C.POINTER(C.c_int64)]),
+    "gb_plan_device_status": (C.c_int, [_VP, C.POINTER(C.c_int32), _VP]),
     "gb_plan_export_index": (C.c_int, [_VP, _VP, _VP]),
     "gb_grid_f32": (C.c_int, [_VP, _VP, _VP, _VP, _VP]),
     "gb_degrid_f32": (C.c_int, [_VP, _VP, _VP, _VP, C.c_int32, _VP]),

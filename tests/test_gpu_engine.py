@@ -127,7 +127,8 @@ def test_plain_fp64_grid_and_degrid():
 
 
 @pytest.mark.parametrize("tile,threads,cap", [(32, 256, 32), (16, 128, 16), (64, 512, 32),
-                                              (8, 256, 8), (32, 512, 64)])
+                                              (8, 256, 8), (32, 512, 64), (25, 256, 32),
+                                              (9, 128, 16)])
 def test_fp32_tiled_grid_matches_fp64_oracle(tile, threads, cap):
     torch = torch_mod()
     c = random_case(3, supports=(8, 12, 30, 7, 1, 40, 70))
@@ -146,6 +147,9 @@ def test_fp32_tiled_grid_matches_fp64_oracle(tile, threads, cap):
     for mode in (0, 1):
         pred = P.degrid(d_gcf, d_model, mode=mode).cpu().numpy()
         assert rel_l2(pred, oracle_degrid(c, model, mode)) < TOL32
+    # even tile edges stage the grid regions with TMA, odd ones with
+    # per-thread copies; no stage wait ran out
+    assert P.device_status() == (0, int(tile % 2 == 0))
 
 
 def test_fp32_adjoint_identity():
