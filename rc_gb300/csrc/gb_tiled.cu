@@ -28,6 +28,7 @@
 #include <algorithm>
 #include <cstring>
 #include <mutex>
+#include <type_traits>
 
 #include "gb_common.cuh"
 #include "gb_plan.cuh"
@@ -400,10 +401,30 @@ __device__ __forceinline__ const CUtensorMap* stage_map(const StageMaps& sm, int
   return c == 0 ? &sm.m[0] : c == 1 ? &sm.m[1] : c == 2 ? &sm.m[2] : &sm.m[3];
 }
 
+// One tap of degridding added into the running group sums by two FMAs per
+// component: MODE 0 adds x * conj(c) (the adjoint of gridding); MODE 1 adds
+// x * c, negated once at the end (the reference's -sum grid * gcf).
+template <int MODE>
+__device__ __forceinline__ void tap_fma(float& br, float& bi, float2 x, float cr, float ci) {
+  if (MODE == 0) {
+    br = fmaf(x.x, cr, br);
+    br = fmaf(x.y, ci, br);
+    bi = fmaf(x.y, cr, bi);
+    bi = fmaf(-x.x, ci, bi);
+  } else {
+    br = fmaf(x.x, cr, br);
+    br = fmaf(-x.y, ci, br);
+    bi = fmaf(x.x, ci, bi);
+    bi = fmaf(x.y, cr, bi);
+  }
+}
+
 // Degridding of one item: stage the A x A grid region, then batches of L
 // decoded records; sub-warps of SW lanes take one piece each (32/SW pieces
-// per warp at a time), lanes stride the piece's taps by SW, Kahan per lane,
-// shuffle reduction within the sub-warp.
+// per warp at a time), lanes stride the piece's taps by SW in groups of four
+// steps; a group's products are summed by FMA chains and the group sum is
+// added to the lane's Kahan accumulator (so the compensated error bound does
+// not grow with the number of taps); shuffle reduction within the sub-warp.
 template <int MODE, int SW, bool TMA>
 __device__ __forceinline__ void degrid_item(const TiledArgs& a, const Item& it, int lt, int L,
                                             int bar, bool whole, int A, float2* __restrict__ sg,
@@ -507,8 +528,11 @@ __device__ __forceinline__ void degrid_item(const TiledArgs& a, const Item& it, 
           const int tot = w2 * r.wy;
           const int n = tot > sl ? (tot - sl + SW - 1) / SW : 0;
           constexpr int UN = 4;
-          for (int t = 0; t < n; t += UN) {
-            // positions first, then every load of the group, then the sums
+          // one group of UN steps: positions first, then every load, then the
+          // sums; CHECK only for the last, partial group (a missing step adds
+          // zeros)
+          auto group = [&](int t, auto check) {
+            constexpr bool CHECK = decltype(check)::value;
             int off_g[UN], off_s[UN];
 #pragma unroll
             for (int u = 0; u < UN; u++) {
@@ -525,62 +549,71 @@ __device__ __forceinline__ void degrid_item(const TiledArgs& a, const Item& it, 
             float2 x0[UN], x1[UN];
 #pragma unroll
             for (int u = 0; u < UN; u++) {
-              const bool ok = t + u < n;
+              const bool ok = !CHECK || t + u < n;
               c[u] = ok ? __ldg(gp + off_g[u]) : make_float4(0.f, 0.f, 0.f, 0.f);
               x0[u] = ok ? sp[off_s[u]] : make_float2(0.f, 0.f);
               x1[u] = ok ? sp[off_s[u] + 1] : make_float2(0.f, 0.f);
             }
+            // the group's products summed by FMA chains, then one compensated
+            // add of the group sum
+            float br = 0.f, bi = 0.f;
 #pragma unroll
             for (int u = 0; u < UN; u++) {
-              if (t + u < n) {
-                float pr0, pi0, pr1, pi1;
-                if (MODE == 0) {  // x * conj(c)
-                  pr0 = x0[u].x * c[u].x + x0[u].y * c[u].y;
-                  pi0 = x0[u].y * c[u].x - x0[u].x * c[u].y;
-                  pr1 = x1[u].x * c[u].z + x1[u].y * c[u].w;
-                  pi1 = x1[u].y * c[u].z - x1[u].x * c[u].w;
-                } else {  // -(x * c)
-                  pr0 = -(x0[u].x * c[u].x - x0[u].y * c[u].y);
-                  pi0 = -(x0[u].x * c[u].y + x0[u].y * c[u].x);
-                  pr1 = -(x1[u].x * c[u].z - x1[u].y * c[u].w);
-                  pi1 = -(x1[u].x * c[u].w + x1[u].y * c[u].z);
-                }
-                kahan(ar, cr, pr0);
-                kahan(ai, ci, pi0);
-                kahan(ar, cr, pr1);
-                kahan(ai, ci, pi1);
-              }
+              tap_fma<MODE>(br, bi, x0[u], c[u].x, c[u].y);
+              tap_fma<MODE>(br, bi, x1[u], c[u].z, c[u].w);
             }
-          }
+            kahan(ar, cr, br);
+            kahan(ai, ci, bi);
+          };
+          int t = 0;
+          for (; t + UN <= n; t += UN) group(t, std::false_type{});
+          if (t < n) group(t, std::true_type{});
         } else {
           const float2* gp = gcf + r.gcf;
-          const int wx = r.wx;
+          const int wx = r.wx, pitch = r.pitch;
           int i = sl - j * wx;
-#pragma unroll 4
-          for (; j < r.wy;) {
-            const float2 c = __ldg(gp + j * r.pitch + i);
-            const float2 x = sp[j * Ae + i];
-            float pr, pi;
-            if (MODE == 0) {  // x * conj(c)
-              pr = x.x * c.x + x.y * c.y;
-              pi = x.y * c.x - x.x * c.y;
-            } else {  // -(x * c)
-              pr = -(x.x * c.x - x.y * c.y);
-              pi = -(x.x * c.y + x.y * c.x);
+          // this lane's taps: sl, sl + SW, ... below wx * wy
+          const int tot = wx * r.wy;
+          const int n = tot > sl ? (tot - sl + SW - 1) / SW : 0;
+          constexpr int UN = 4;
+          auto group = [&](int t, auto check) {
+            constexpr bool CHECK = decltype(check)::value;
+            int off_g[UN], off_s[UN];
+#pragma unroll
+            for (int u = 0; u < UN; u++) {
+              off_g[u] = j * pitch + i;
+              off_s[u] = j * Ae + i;
+              i += di;
+              j += dj;
+              if (i >= wx) {
+                i -= wx;
+                j++;
+              }
             }
-            kahan(ar, cr, pr);
-            kahan(ai, ci, pi);
-            i += di;
-            j += dj;
-            if (i >= wx) {
-              i -= wx;
-              j++;
+            float2 c[UN], x[UN];
+#pragma unroll
+            for (int u = 0; u < UN; u++) {
+              const bool ok = !CHECK || t + u < n;
+              c[u] = ok ? __ldg(gp + off_g[u]) : make_float2(0.f, 0.f);
+              x[u] = ok ? sp[off_s[u]] : make_float2(0.f, 0.f);
             }
-          }
+            float br = 0.f, bi = 0.f;
+#pragma unroll
+            for (int u = 0; u < UN; u++) tap_fma<MODE>(br, bi, x[u], c[u].x, c[u].y);
+            kahan(ar, cr, br);
+            kahan(ai, ci, bi);
+          };
+          int t = 0;
+          for (; t + UN <= n; t += UN) group(t, std::false_type{});
+          if (t < n) group(t, std::true_type{});
         }
       }
       ar -= cr;
       ai -= ci;
+      if (MODE == 1) {  // the reference's negated product
+        ar = -ar;
+        ai = -ai;
+      }
 #pragma unroll
       for (int o = SW / 2; o > 0; o >>= 1) {
         ar += __shfl_xor_sync(0xffffffffu, ar, o);
