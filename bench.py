@@ -280,7 +280,7 @@ def our_arm(args):
     from rc_gb300 import autotune as AT
 
     explicit = {k: v for k, v in (("tile", args.tile), ("threads", args.threads),
-                                  ("period_cap", args.cap)) if v}
+                                  ("period_cap", args.cap), ("bundles_per_cta", args.bpc)) if v}
     tune_info = {"source": "flags" if explicit else "autotune"}
     if explicit or args.no_tune:
         params = dict(AT.DEFAULT, **explicit)
@@ -501,7 +501,11 @@ def our_arm(args):
             "rel_l2_vs_fp64": {"grid": err_grid, "degrid": err_deg, "bar": 1e-5},
             "e2e": {"value": round(e2e_mvis, 3), "unit": "Mvis/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h,
-                    "ms_per_step": round(float(np.mean(e2e)), 3) if e2e else None},
+                    "ms_per_step": round(float(np.mean(e2e)), 3) if e2e else None,
+                    # the copies cross the host link, which other jobs on the
+                    # machine may share: the spread shows a disturbed run
+                    "ms_median": round(float(np.median(e2e)), 3) if e2e else None,
+                    "ms_max": round(float(np.max(e2e)), 3) if e2e else None},
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
             "gpu_launches": 2 * args.steps,
@@ -949,6 +953,7 @@ def main(argv=None):
     ap.add_argument("--tile", type=int, default=0)
     ap.add_argument("--threads", type=int, default=0)
     ap.add_argument("--cap", type=int, default=0)
+    ap.add_argument("--bpc", type=int, default=0, help="bundles per CTA (0: tuned)")
     ap.add_argument("--no-graph", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="built-in defaults, no autotuning")
     ap.add_argument("--no-cpu", action="store_true")
