@@ -153,13 +153,30 @@ int gb_plan_destroy(gb_plan *plan);
  * [5] largest support, [6] threads per CTA. */
 int gb_plan_stats(const gb_plan *plan, int64_t *stats7);
 
+/* How FP32 degridding stages each tile's grid region in shared memory:
+ *   GB_STAGE_SPLIT: per-thread asynchronous copies into rows split into their
+ *     even and then their odd pixels, so the two taps of a pair are read by
+ *     two loads contiguous across the lanes (best when most taps are paired:
+ *     even supports, a 16-byte aligned GCF);
+ *   GB_STAGE_TMA: one 2-D TMA copy per region, rows as in the grid (single
+ *     grid, even tile edge, even row pitch, 16-byte aligned grid);
+ *   GB_STAGE_ROWS: per-thread asynchronous copies, rows as in the grid.
+ * GB_STAGE_AUTO (the default) takes SPLIT when at least half of the plan's
+ * taps are paired and the GCF is 16-byte aligned, otherwise TMA where it
+ * applies, otherwise ROWS.  A forced TMA falls back to ROWS where TMA does
+ * not apply. */
+#define GB_STAGE_AUTO (-1)
+#define GB_STAGE_SPLIT 0
+#define GB_STAGE_TMA 1
+#define GB_STAGE_ROWS 2
+int gb_plan_set_stage(gb_plan *plan, int32_t stage);
+
 /* Device-side status of a plan's degridding, read synchronously on `stream`:
  * out2[0] = 1 when a TMA stage of a degridding launch did not complete within
  * its bounded wait since the last call (that launch's predictions are then
- * invalid; the word is cleared by this call), out2[1] = 1 when the last
- * degridding launch staged its grid regions with TMA (single grid, even tile
- * edge, even row pitch, 16-byte aligned grid), 0 when it used per-thread
- * asynchronous copies.  Returns GB_ERR_TIMEOUT when out2[0] is set. */
+ * invalid; the word is cleared by this call), out2[1] = the GB_STAGE_* form
+ * the last degridding launch used.  Returns GB_ERR_TIMEOUT when out2[0] is
+ * set. */
 int gb_plan_device_status(gb_plan *plan, int32_t *out2, void *stream);
 
 /* Per-visibility index record (x0, y0, phase ou+8*ov, plane, kept) as the

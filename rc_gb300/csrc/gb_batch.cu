@@ -25,14 +25,15 @@ struct gb_batch {
   int n_classes = 0;
   gb::ClassInfo cls[gb::kMaxClasses] = {};
   size_t smem_grid = 0, smem_degrid = 0;
-  int ctas_grid = 1, ctas_degrid = 1;
+  int ctas_grid = 1;
+  int ctas_degrid[3] = {1, 1, 1};  // per staging form (split and rows are used)
   gb::Rec* d_recs = nullptr;
   gb::Item* d_items = nullptr;
   gb::Bundle* d_bundles = nullptr;
   int32_t* d_queue = nullptr;
   int64_t n_recs = 0;
   int n_items = 0, n_bundles = 0;
-  int64_t kept = 0, taps = 0;
+  int64_t kept = 0, taps = 0, taps_paired = 0;
 };
 
 using namespace gb;
@@ -99,7 +100,7 @@ static int batch_build(gb_batch* B, int32_t n, const gb_batch_member* m, cudaStr
   B->smem_grid = tiled_smem_grid(B->cls, B->n_classes, B->NT);
   B->smem_degrid = tiled_smem_degrid(B->cls, B->n_classes, B->NT);
   B->ctas_grid = tiled_ctas_per_sm_for(B->NT, true, B->smem_grid);
-  B->ctas_degrid = tiled_ctas_per_sm_for(B->NT, false, B->smem_degrid);
+  for (int st : {0, 2}) B->ctas_degrid[st] = tiled_ctas_per_sm_for(B->NT, false, B->smem_degrid, st);
 
   // merged records and items
   std::vector<HostItem> items;
@@ -117,6 +118,7 @@ static int batch_build(gb_batch* B, int32_t n, const gb_batch_member* m, cudaStr
     off += p->n_recs;
     B->kept += p->kept;
     B->taps += p->taps;
+    B->taps_paired += p->taps_paired;
   }
   B->n_recs = off;
   if (B->n_recs >= (int64_t)INT32_MAX) {
@@ -221,7 +223,7 @@ extern "C" int gb_batch_grid_f32(gb_batch* B, const float* const* d_vis, const f
   if (rc) return rc;
   return launch_tiled_batch(true, 0, B->NT, B->smem_grid, B->ctas_grid, B->d_bundles,
                             B->n_bundles, B->d_items, B->d_recs, B->d_queue, B->cls,
-                            B->n_classes, B->T, gp, d_gcf, (cudaStream_t)stream);
+                            B->n_classes, B->T, gp, d_gcf, 0, (cudaStream_t)stream);
 }
 
 extern "C" int gb_batch_degrid_f32(gb_batch* B, const float* d_gcf, const float* const* d_grids,
@@ -237,9 +239,11 @@ extern "C" int gb_batch_degrid_f32(gb_batch* B, const float* d_gcf, const float*
   for (size_t i = 0; i < B->members.size(); i++)
     if (B->members[i]->dev.n_vis)
       GB_CUDA_TRY(cudaMemsetAsync(d_preds[i], 0, sizeof(float2) * B->members[i]->dev.n_vis, s));
-  return launch_tiled_batch(false, mode, B->NT, B->smem_degrid, B->ctas_degrid, B->d_bundles,
+  // several grids: no TMA; split rows when most taps are paired
+  const int stage = degrid_stage_choice(-1, B->taps, B->taps_paired, d_gcf, false);
+  return launch_tiled_batch(false, mode, B->NT, B->smem_degrid, B->ctas_degrid[stage], B->d_bundles,
                             B->n_bundles, B->d_items, B->d_recs, B->d_queue, B->cls,
-                            B->n_classes, B->T, gp, d_gcf, s);
+                            B->n_classes, B->T, gp, d_gcf, stage, s);
 }
 
 // Plain FP64 path over the members (one launch each): the comparison path of

@@ -29,10 +29,10 @@ __global__ void k_plan_count(PlanDev P, const PlaneInfo* __restrict__ pl,
                              int32_t n_planes, double w_lo, double w_hi, int32_t T, int32_t ntx,
                              int32_t nper, int32_t* __restrict__ hist,
                              unsigned long long* __restrict__ counters) {
-  __shared__ unsigned long long s_kept, s_taps, s_recs;
-  if (threadIdx.x == 0) s_kept = s_taps = s_recs = 0ull;
+  __shared__ unsigned long long s_kept, s_taps, s_recs, s_paired;
+  if (threadIdx.x == 0) s_kept = s_taps = s_recs = s_paired = 0ull;
   __syncthreads();
-  unsigned long long kept = 0, taps = 0, recs = 0;
+  unsigned long long kept = 0, taps = 0, recs = 0, paired = 0;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < P.n_vis;
        t += (int64_t)gridDim.x * blockDim.x) {
     const double* r = P.uvw + t * P.uvw_stride;
@@ -55,17 +55,24 @@ __global__ void k_plan_count(PlanDev P, const PlaneInfo* __restrict__ pl,
         const int64_t tile = (int64_t)(Y0 / T) * ntx + (X0 / T);
         atomicAdd(&hist[tile * nper + q.rank], 1);
         recs++;
+        // degridding pairs the taps of a piece whose rows, GCF rows and GCF
+        // offset are all even (the same rule the kernels apply per record)
+        const int wx = min(q.P, q.S - kx * q.P), wy = min(q.P, q.S - ky * q.P);
+        if (((wx | q.S | (int)((q.gcf_off + kx * q.P) & 1)) & 1) == 0)
+          paired += (unsigned long long)wx * wy;
       }
     }
   }
   atomicAdd(&s_kept, kept);
   atomicAdd(&s_taps, taps);
   atomicAdd(&s_recs, recs);
+  atomicAdd(&s_paired, paired);
   __syncthreads();
   if (threadIdx.x == 0) {
     atomicAdd(&counters[0], s_kept);
     atomicAdd(&counters[1], s_taps);
     atomicAdd(&counters[2], s_recs);
+    atomicAdd(&counters[3], s_paired);
   }
 }
 
@@ -272,8 +279,7 @@ static int build_plan(gb_plan* P, const gb_geometry* geo, int64_t n_vis, const d
   P->smem_grid = tiled_smem_grid(P->cls, P->n_classes, P->NT);
   P->smem_degrid = tiled_smem_degrid(P->cls, P->n_classes, P->NT);
   P->ctas_per_sm_grid = tiled_ctas_per_sm(P, true);
-  P->ctas_per_sm_degrid = tiled_ctas_per_sm(P, false);
-  P->ctas_per_sm_degrid_tma = tiled_ctas_per_sm(P, false, true);
+  for (int st = 0; st < 3; st++) P->ctas_per_sm_degrid[st] = tiled_ctas_per_sm(P, false, st);
 
   // ---- device tables
   if ((rc = dalloc(&P->d_plane, n_vis)) || (rc = dalloc(&P->d_supports, np)) ||
@@ -314,7 +320,7 @@ static int build_plan(gb_plan* P, const gb_geometry* geo, int64_t n_vis, const d
   int32_t *d_hist = nullptr, *d_offs = nullptr;
   unsigned long long* d_cnt = nullptr;
   if ((rc = dalloc(&d_hist, nkeys)) || (rc = dalloc(&d_offs, nkeys + 1)) ||
-      (rc = dalloc(&d_cnt, 3))) {
+      (rc = dalloc(&d_cnt, 4))) {
     cudaFree(d_hist);
     cudaFree(d_offs);
     cudaFree(d_cnt);
@@ -327,7 +333,7 @@ static int build_plan(gb_plan* P, const gb_geometry* geo, int64_t n_vis, const d
     }
   } tmp{{d_hist, d_offs, d_cnt}};
   GB_CUDA_TRY(cudaMemsetAsync(d_hist, 0, sizeof(int32_t) * nkeys, s));
-  GB_CUDA_TRY(cudaMemsetAsync(d_cnt, 0, sizeof(unsigned long long) * 3, s));
+  GB_CUDA_TRY(cudaMemsetAsync(d_cnt, 0, sizeof(unsigned long long) * 4, s));
   if (n_vis > 0) {
     k_plan_count<<<blocks_for(n_vis, 256), 256, 0, s>>>(
         D, P->d_planes, d_plane_in, P->d_plane, np, geo->w_low, geo->w_high, P->T, P->ntx, nper,
@@ -335,7 +341,7 @@ static int build_plan(gb_plan* P, const gb_geometry* geo, int64_t n_vis, const d
     GB_CUDA_TRY(cudaGetLastError());
   }
   std::vector<int32_t> hist(nkeys);
-  unsigned long long cnt[3];
+  unsigned long long cnt[4];
   GB_CUDA_TRY(cudaMemcpyAsync(hist.data(), d_hist, sizeof(int32_t) * nkeys, cudaMemcpyDeviceToHost,
                               s));
   GB_CUDA_TRY(cudaMemcpyAsync(cnt, d_cnt, sizeof(cnt), cudaMemcpyDeviceToHost, s));
@@ -343,6 +349,7 @@ static int build_plan(gb_plan* P, const gb_geometry* geo, int64_t n_vis, const d
   P->kept = (int64_t)cnt[0];
   P->taps = (int64_t)cnt[1];
   P->n_recs = (int64_t)cnt[2];
+  P->taps_paired = (int64_t)cnt[3];
   if (P->n_recs >= (int64_t)INT32_MAX) {
     gb_set_error(GB_ERR_CAPACITY, "more than 2^31 footprint pieces");
     return GB_ERR_CAPACITY;
@@ -541,6 +548,15 @@ extern "C" int gb_plan_stats(const gb_plan* P, int64_t* st) {
   return GB_OK;
 }
 
+extern "C" int gb_plan_set_stage(gb_plan* P, int32_t stage) {
+  if (!P || stage < GB_STAGE_AUTO || stage > GB_STAGE_ROWS) {
+    gb_set_error(GB_ERR_ARG, "gb_plan_set_stage: bad argument");
+    return GB_ERR_ARG;
+  }
+  P->stage_pref = stage;
+  return GB_OK;
+}
+
 extern "C" int gb_plan_device_status(gb_plan* P, int32_t* out2, void* stream) {
   if (!P || !out2) {
     gb_set_error(GB_ERR_ARG, "gb_plan_device_status: NULL argument");
@@ -552,7 +568,7 @@ extern "C" int gb_plan_device_status(gb_plan* P, int32_t* out2, void* stream) {
   GB_CUDA_TRY(cudaMemsetAsync(P->d_queue + 2, 0, sizeof(int32_t), s));
   GB_CUDA_TRY(cudaStreamSynchronize(s));
   out2[0] = err;
-  out2[1] = P->last_stage_tma;
+  out2[1] = P->last_stage;
   if (err) {
     gb_set_error(GB_ERR_TIMEOUT, "degridding: a TMA stage did not complete in time");
     return GB_ERR_TIMEOUT;

@@ -136,7 +136,8 @@ struct gb_plan {
   int n_classes = 0;
   gb::ClassInfo cls[gb::kMaxClasses] = {};
   size_t smem_grid = 0, smem_degrid = 0;
-  int ctas_per_sm_grid = 1, ctas_per_sm_degrid = 1, ctas_per_sm_degrid_tma = 1;
+  int ctas_per_sm_grid = 1;
+  int ctas_per_sm_degrid[3] = {1, 1, 1};  // per GB_STAGE_* form
   // device arrays owned by the plan
   int32_t* d_plane = nullptr;
   int32_t* d_supports = nullptr;
@@ -149,6 +150,8 @@ struct gb_plan {
   int64_t n_recs = 0;
   int n_items = 0, n_bundles = 0;
   int64_t kept = 0, taps = 0, tiles_used = 0;
+  int64_t taps_paired = 0;  // taps of pieces that degridding can take in pairs
+  int stage_pref = -1;      // GB_STAGE_*: forced staging form of degridding, or -1
   bool own_plane = true;
   std::vector<gb::HostItem> host_items;  // in d_items order (grid slot 0)
   // TMA descriptors of the last degridded grid, one per thread-group class
@@ -158,7 +161,7 @@ struct gb_plan {
   int64_t tma_pitch = 0;
   bool tma_ok = false;
   CUtensorMap tma_maps[gb::kMaxClasses];
-  int last_stage_tma = 0;  // 1: the last degridding launch staged with TMA
+  int last_stage = 0;  // GB_STAGE_* form of the last degridding launch
 };
 
 namespace gb {
@@ -186,8 +189,12 @@ int launch_grid_tiled_tables(const Bundle* bundles, int n_bundles, const Item* i
 int launch_tiled_batch(bool grid_mode, int mode, int NT, size_t smem, int ctas_per_sm,
                        const Bundle* bundles, int n_bundles, const Item* items, const Rec* recs,
                        int32_t* queue, const ClassInfo* cls, int n_classes, int T,
-                       const GridPtrs& gp, const float* gcf, cudaStream_t s);
-int tiled_ctas_per_sm_for(int NT, bool grid, size_t smem);
-// Resident CTAs per SM of the tiled grid (or degrid) kernel for this plan.
-int tiled_ctas_per_sm(const gb_plan* plan, bool grid, bool tma = false);
+                       const GridPtrs& gp, const float* gcf, int stage, cudaStream_t s);
+// Staging form of a degridding launch (GB_STAGE_SPLIT / _TMA / _ROWS): split
+// rows when at least half of the taps are paired and the GCF allows pairs.
+int degrid_stage_choice(int pref, int64_t taps, int64_t taps_paired, const float* gcf,
+                        bool tma_possible);
+int tiled_ctas_per_sm_for(int NT, bool grid, size_t smem, int stage = 0);
+// Resident CTAs per SM of the tiled grid (or degrid, per staging form) kernel.
+int tiled_ctas_per_sm(const gb_plan* plan, bool grid, int stage = 0);
 }  // namespace gb

@@ -94,9 +94,10 @@ struct __align__(16) DegridRec {
   int16_t dj, di;  // a sub-warp's stride through the piece: SW steps = dj rows + di steps
   float rcp_w;     // 1 / (steps per row), for each lane's first step without a division
   int32_t flags;   // kRecCut: footprint cut into pieces (accumulate with atomics);
-                   // kRecPaired: a step is two adjacent taps (one 16-byte GCF load)
+                   // kRecPaired: a step is two adjacent taps (one 16-byte GCF load);
+                   // kRecOdd: the piece's first column is odd; bits 8-15: that column
 };
-constexpr int32_t kRecCut = 1, kRecPaired = 2;
+constexpr int32_t kRecCut = 1, kRecPaired = 2, kRecOdd = 4;
 static_assert(sizeof(DegridRec) == 32, "DegridRec is two 16-byte words");
 
 // Residue slots a thread needs for period P in a group of L threads.
@@ -425,7 +426,10 @@ __device__ __forceinline__ void tap_fma(float& br, float& bi, float2 x, float cr
 // steps; a group's products are summed by FMA chains and the group sum is
 // added to the lane's Kahan accumulator (so the compensated error bound does
 // not grow with the number of taps); shuffle reduction within the sub-warp.
-template <int MODE, int SW, bool TMA>
+// Staging forms (the GB_STAGE_* values of the C API).
+constexpr int kStageSplit = 0, kStageTma = 1, kStageRows = 2;
+
+template <int MODE, int SW, int STAGE>
 __device__ __forceinline__ void degrid_item(const TiledArgs& a, const Item& it, int lt, int L,
                                             int bar, bool whole, int A, float2* __restrict__ sg,
                                             DegridRec* __restrict__ srec, const GridSlot& gs,
@@ -433,7 +437,13 @@ __device__ __forceinline__ void degrid_item(const TiledArgs& a, const Item& it, 
                                             const StageMaps& sm, int cls, int slot) {
   const float2* __restrict__ grid = gs.grid;
   float2* __restrict__ pred = gs.vis;
+  constexpr bool TMA = STAGE == kStageTma, SPLIT = STAGE == kStageSplit;
   const int Ae = stage_stride(A);  // stage row stride (even)
+  // TMA and ROWS stage rows as they lie in the grid.  SPLIT stores each row
+  // as its even pixels, then its odd pixels (He = Ae / 2 each), so the two
+  // taps of a pair are read by two loads that are each contiguous across the
+  // lanes, whatever the parity of the piece's first column.
+  const int He = Ae >> 1;
   const int x0 = it.tile_x * a.T, y0 = it.tile_y * a.T;
   if constexpr (TMA) {
     if (lt == 0) {
@@ -451,6 +461,7 @@ __device__ __forceinline__ void degrid_item(const TiledArgs& a, const Item& it, 
     for (int q = lt; q < AA; q += L) {
       const int gx = x0 + px, gy = y0 + py;
       const bool in = px < A && gx < gs.ext_x && gy < gs.ext_y;
+      const int sq = SPLIT ? py * Ae + (px & 1) * He + (px >> 1) : q;
       px += dx;
       py += dy;
       if (px >= Ae) {
@@ -458,7 +469,7 @@ __device__ __forceinline__ void degrid_item(const TiledArgs& a, const Item& it, 
         py++;
       }
       const float2* src = in ? grid + (int64_t)gy * gs.pitch + gx : grid;
-      const unsigned dst = (unsigned)__cvta_generic_to_shared(sg + q);
+      const unsigned dst = (unsigned)__cvta_generic_to_shared(sg + sq);
       asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(dst), "l"(src),
                    "r"(in ? 8 : 0)
                    : "memory");
@@ -477,7 +488,6 @@ __device__ __forceinline__ void degrid_item(const TiledArgs& a, const Item& it, 
       const Rec r = a.recs[base + lt];
       DegridRec d;
       d.gcf = (int32_t)r.gcf;
-      d.q0 = r.yl * Ae + r.xl;
       d.pitch = r.sm1 + 1;
       d.vis = r.vis;
       d.wx = r.wx;
@@ -489,7 +499,14 @@ __device__ __forceinline__ void degrid_item(const TiledArgs& a, const Item& it, 
       d.dj = (int16_t)(SW / steps);
       d.di = (int16_t)(SW - d.dj * steps);
       d.rcp_w = 1.0f / (float)steps;
-      d.flags = (r.sm1 > r.pm1 ? kRecCut : 0) | (paired ? kRecPaired : 0);
+      d.flags = (r.sm1 > r.pm1 ? kRecCut : 0) | (paired ? kRecPaired : 0) |
+                (r.xl & 1 ? kRecOdd : 0) | ((int32_t)r.xl << 8);
+      // stage offset of the piece's first tap (row-major), or in the split
+      // layout: of its first tap for pairs, of its first row for single taps
+      if constexpr (SPLIT)
+        d.q0 = r.yl * Ae + (paired ? (r.xl & 1) * He + (r.xl >> 1) : 0);
+      else
+        d.q0 = r.yl * Ae + r.xl;
       srec[lt] = d;
     }
     // the stage (issued before the first batch's record loads, so the two
@@ -523,6 +540,9 @@ __device__ __forceinline__ void degrid_item(const TiledArgs& a, const Item& it, 
         if (r.flags & kRecPaired) {
           const int w2 = r.wx >> 1, p2 = r.pitch >> 1;
           const float4* gp = reinterpret_cast<const float4*>(gcf + r.gcf);
+          // the pair's second tap: the next pixel (row-major), or the other
+          // half of the split row (one column on when the first is odd)
+          const float2* sp1 = SPLIT ? sp + ((r.flags & kRecOdd) ? 1 - He : He) : sp + 1;
           int i = sl - j * w2;
           // this lane's pairs: sl, sl + SW, ... below w2 * wy (SW is a power of two)
           const int tot = w2 * r.wy;
@@ -537,7 +557,7 @@ __device__ __forceinline__ void degrid_item(const TiledArgs& a, const Item& it, 
 #pragma unroll
             for (int u = 0; u < UN; u++) {
               off_g[u] = j * p2 + i;
-              off_s[u] = j * Ae + 2 * i;
+              off_s[u] = j * Ae + (SPLIT ? i : 2 * i);
               i += di;
               j += dj;
               if (i >= w2) {
@@ -552,7 +572,7 @@ __device__ __forceinline__ void degrid_item(const TiledArgs& a, const Item& it, 
               const bool ok = !CHECK || t + u < n;
               c[u] = ok ? __ldg(gp + off_g[u]) : make_float4(0.f, 0.f, 0.f, 0.f);
               x0[u] = ok ? sp[off_s[u]] : make_float2(0.f, 0.f);
-              x1[u] = ok ? sp[off_s[u] + 1] : make_float2(0.f, 0.f);
+              x1[u] = ok ? sp1[off_s[u]] : make_float2(0.f, 0.f);
             }
             // the group's products summed by FMA chains, then one compensated
             // add of the group sum
@@ -570,7 +590,7 @@ __device__ __forceinline__ void degrid_item(const TiledArgs& a, const Item& it, 
           if (t < n) group(t, std::true_type{});
         } else {
           const float2* gp = gcf + r.gcf;
-          const int wx = r.wx, pitch = r.pitch;
+          const int wx = r.wx, pitch = r.pitch, xl = (r.flags >> 8) & 0xFF;
           int i = sl - j * wx;
           // this lane's taps: sl, sl + SW, ... below wx * wy
           const int tot = wx * r.wy;
@@ -582,7 +602,12 @@ __device__ __forceinline__ void degrid_item(const TiledArgs& a, const Item& it, 
 #pragma unroll
             for (int u = 0; u < UN; u++) {
               off_g[u] = j * pitch + i;
-              off_s[u] = j * Ae + i;
+              if constexpr (SPLIT) {
+                const int c = xl + i;
+                off_s[u] = j * Ae + (c & 1) * He + (c >> 1);
+              } else {
+                off_s[u] = j * Ae + i;
+              }
               i += di;
               j += dj;
               if (i >= wx) {
@@ -631,7 +656,7 @@ __device__ __forceinline__ void degrid_item(const TiledArgs& a, const Item& it, 
 
 // At most 64 registers per thread (1024 resident threads per SM): registers
 // then do not cut the CTAs per SM below what shared memory allows.
-template <int NT, int MODE, bool TMA>
+template <int NT, int MODE, int STAGE>
 __global__ void __launch_bounds__(NT, 1024 / NT)
     k_degrid_tiled(const __grid_constant__ TiledArgs a, const __grid_constant__ GridPtrs gp,
                    const __grid_constant__ StageMaps sm, const float2* __restrict__ gcf) {
@@ -639,7 +664,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT)
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ int s_b;
   const int tid = threadIdx.x;
-  if constexpr (TMA) {
+  if constexpr (STAGE == kStageTma) {
     if (tid < NT / 64) mbar_init(&g_stage_bar[tid], 1);
     if (tid == 0) g_stage_phase = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -662,13 +687,13 @@ __global__ void __launch_bounds__(NT, 1024 / NT)
       const bool whole = ci.L == NT;
       // sub-warp width by piece size: <= 64 taps -> 8 lanes, <= 256 -> 16, else 32
       if (ci.pmax <= 8)
-        degrid_item<MODE, 8, TMA>(a, it, lt, ci.L, 1 + g, whole, ci.A, sg, srec,
+        degrid_item<MODE, 8, STAGE>(a, it, lt, ci.L, 1 + g, whole, ci.A, sg, srec,
                                    gp.s[bd.grid], gcf, sm, bd.cls, g);
       else if (ci.pmax <= 16)
-        degrid_item<MODE, 16, TMA>(a, it, lt, ci.L, 1 + g, whole, ci.A, sg, srec,
+        degrid_item<MODE, 16, STAGE>(a, it, lt, ci.L, 1 + g, whole, ci.A, sg, srec,
                                    gp.s[bd.grid], gcf, sm, bd.cls, g);
       else
-        degrid_item<MODE, 32, TMA>(a, it, lt, ci.L, 1 + g, whole, ci.A, sg, srec,
+        degrid_item<MODE, 32, STAGE>(a, it, lt, ci.L, 1 + g, whole, ci.A, sg, srec,
                                    gp.s[bd.grid], gcf, sm, bd.cls, g);
     }
     __syncthreads();
@@ -708,15 +733,27 @@ static GridFn grid_fn(int NT) {
   return NT == 128 ? k_grid_tiled<128> : NT == 256 ? k_grid_tiled<256> : k_grid_tiled<512>;
 }
 
-template <bool TMA>
+template <int STAGE>
 static DegridFn degrid_fn_t(int NT, int mode) {
-  if (NT == 128) return mode ? k_degrid_tiled<128, 1, TMA> : k_degrid_tiled<128, 0, TMA>;
-  if (NT == 256) return mode ? k_degrid_tiled<256, 1, TMA> : k_degrid_tiled<256, 0, TMA>;
-  return mode ? k_degrid_tiled<512, 1, TMA> : k_degrid_tiled<512, 0, TMA>;
+  if (NT == 128) return mode ? k_degrid_tiled<128, 1, STAGE> : k_degrid_tiled<128, 0, STAGE>;
+  if (NT == 256) return mode ? k_degrid_tiled<256, 1, STAGE> : k_degrid_tiled<256, 0, STAGE>;
+  return mode ? k_degrid_tiled<512, 1, STAGE> : k_degrid_tiled<512, 0, STAGE>;
 }
 
-static DegridFn degrid_fn(int NT, int mode, bool tma = false) {
-  return tma ? degrid_fn_t<true>(NT, mode) : degrid_fn_t<false>(NT, mode);
+static DegridFn degrid_fn(int NT, int mode, int stage) {
+  return stage == kStageTma    ? degrid_fn_t<kStageTma>(NT, mode)
+         : stage == kStageRows ? degrid_fn_t<kStageRows>(NT, mode)
+                               : degrid_fn_t<kStageSplit>(NT, mode);
+}
+
+int degrid_stage_choice(int pref, int64_t taps, int64_t taps_paired, const float* gcf,
+                        bool tma_possible) {
+  if (pref == kStageTma || pref == kStageRows)
+    return pref == kStageTma && tma_possible ? kStageTma : kStageRows;
+  if (pref == kStageSplit) return kStageSplit;
+  const bool pairs = (reinterpret_cast<uintptr_t>(gcf) & 15) == 0 && 2 * taps_paired >= taps;
+  if (pairs) return kStageSplit;
+  return tma_possible ? kStageTma : kStageRows;
 }
 
 static int set_smem_attr(const void* fn) {
@@ -725,11 +762,11 @@ static int set_smem_attr(const void* fn) {
   return GB_OK;
 }
 
-int tiled_ctas_per_sm(const gb_plan* P, bool grid, bool tma) {
+int tiled_ctas_per_sm(const gb_plan* P, bool grid, int stage) {
   const void* fn = grid ? (const void*)grid_fn(P->NT)
-                        : (const void*)degrid_fn(P->NT, 0, tma);
+                        : (const void*)degrid_fn(P->NT, 0, stage);
   if (set_smem_attr(fn)) return 1;
-  if (!grid) set_smem_attr((const void*)degrid_fn(P->NT, 1, tma));
+  if (!grid) set_smem_attr((const void*)degrid_fn(P->NT, 1, stage));
   int n = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, P->NT,
                                                 grid ? P->smem_grid : P->smem_degrid);
@@ -842,12 +879,15 @@ int launch_degrid_tiled(gb_plan* P, const float* gcf, const float* grid, float* 
   GB_CUDA_TRY(cudaMemsetAsync(P->d_queue + 1, 0, sizeof(int32_t), s));
   StageMaps sm;
   memset(&sm, 0, sizeof(sm));
-  const bool tma = stage_maps(P, grid, &sm);
+  // tensor maps only where the choice can fall on TMA
+  int stage = degrid_stage_choice(P->stage_pref, P->taps, P->taps_paired, gcf, false);
+  if (stage == kStageRows)
+    stage = degrid_stage_choice(P->stage_pref, P->taps, P->taps_paired, gcf,
+                                stage_maps(P, grid, &sm));
   sm.err = P->d_queue + 2;
-  P->last_stage_tma = tma ? 1 : 0;
-  const int per_sm = tma ? P->ctas_per_sm_degrid_tma : P->ctas_per_sm_degrid;
-  const int blocks = std::min(P->n_bundles, sm_count() * per_sm);
-  DegridFn fn = degrid_fn(P->NT, mode, tma);
+  P->last_stage = stage;
+  const int blocks = std::min(P->n_bundles, sm_count() * P->ctas_per_sm_degrid[stage]);
+  DegridFn fn = degrid_fn(P->NT, mode, stage);
   fn<<<blocks, P->NT, P->smem_degrid, s>>>(
       make_args(P), one_grid(grid, pred, P->dev.ext_x, P->dev.ext_y, P->dev.pitch), sm,
       (const float2*)gcf);
@@ -887,7 +927,7 @@ int launch_grid_tiled_tables(const Bundle* bundles, int n_bundles, const Item* i
 int launch_tiled_batch(bool grid_mode, int mode, int NT, size_t smem, int ctas_per_sm,
                        const Bundle* bundles, int n_bundles, const Item* items, const Rec* recs,
                        int32_t* queue, const ClassInfo* cls, int n_classes, int T,
-                       const GridPtrs& gp, const float* gcf, cudaStream_t s) {
+                       const GridPtrs& gp, const float* gcf, int stage, cudaStream_t s) {
   if (n_bundles <= 0) return GB_OK;
   TiledArgs a;
   a.bundles = bundles;
@@ -904,9 +944,9 @@ int launch_tiled_batch(bool grid_mode, int mode, int NT, size_t smem, int ctas_p
     GridFn fn = grid_fn(NT);
     fn<<<blocks, NT, smem, s>>>(a, gp, (const float2*)gcf);
   } else {
-    StageMaps sm;  // several grids: per-thread asynchronous staging
+    StageMaps sm;  // several grids: per-thread asynchronous staging (split or rows)
     memset(&sm, 0, sizeof(sm));
-    DegridFn fn = degrid_fn(NT, mode);
+    DegridFn fn = degrid_fn(NT, mode, stage == kStageSplit ? kStageSplit : kStageRows);
     fn<<<blocks, NT, smem, s>>>(a, gp, sm, (const float2*)gcf);
   }
   GB_CUDA_TRY(cudaGetLastError());
@@ -914,10 +954,10 @@ int launch_tiled_batch(bool grid_mode, int mode, int NT, size_t smem, int ctas_p
 }
 
 // Occupancy of the batched kernels (sets their shared-memory limit first).
-int tiled_ctas_per_sm_for(int NT, bool grid, size_t smem) {
-  const void* fn = grid ? (const void*)grid_fn(NT) : (const void*)degrid_fn(NT, 0);
+int tiled_ctas_per_sm_for(int NT, bool grid, size_t smem, int stage) {
+  const void* fn = grid ? (const void*)grid_fn(NT) : (const void*)degrid_fn(NT, 0, stage);
   if (set_smem_attr(fn)) return 1;
-  if (!grid) set_smem_attr((const void*)degrid_fn(NT, 1));
+  if (!grid) set_smem_attr((const void*)degrid_fn(NT, 1, stage));
   int n = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, NT, smem);
   return n > 0 ? n : 1;

@@ -77,9 +77,15 @@ class Plan:
         keys = ["kept", "taps", "items", "tiles", "tile", "max_support", "threads"]
         return dict(zip(keys, list(st)))
 
+    def set_stage(self, stage):
+        """Force how FP32 degridding stages grid regions (lib.STAGE_SPLIT,
+        STAGE_TMA, STAGE_ROWS) or restore the automatic choice (STAGE_AUTO)."""
+        _lib.check(self.L.gb_plan_set_stage(self.h, int(stage)), "gb_plan_set_stage")
+
     def device_status(self, stream=None):
-        """(error, staged_with_tma) of the last degridding launches: error = 1
-        when a TMA stage did not complete in time (cleared by this call)."""
+        """(error, stage) of the last degridding launches: error = 1 when a
+        TMA stage did not complete in time (cleared by this call); stage = the
+        lib.STAGE_* form the last launch used."""
         out = (C.c_int32 * 2)()
         rc = self.L.gb_plan_device_status(self.h, out, _stream(stream))
         if rc not in (_lib.GB_OK, _lib.ERR_TIMEOUT):

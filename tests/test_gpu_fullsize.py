@@ -4,8 +4,9 @@ Config 2 (4.18 M visibilities, 4096^2 grid, 32 w-planes with supports 8-64,
 oversample 8) goes against the oracle on the whole observation:
 - w-planes and per-visibility indices are bit-exact;
 - the plain FP64 pair is within relative L2 1e-12;
-- the FP32 pair is within 1e-5, for both degridding stage paths (TMA for even
-  tile edges, per-thread copies for odd ones);
+- the FP32 pair is within 1e-5, with degridding's default staging (split
+  rows: every support is even) and with the TMA form (rows as in the grid;
+  per-thread copies on the odd tile edge);
 - the adjoint identity holds to FP32 rounding;
 - the GCFs generated on the GPU match the oracle's generator.
 
@@ -170,7 +171,15 @@ def test_c2_fp32_pair_matches_the_oracle(c2, tile, threads, cap):
     assert rel_l2(grid.cpu().numpy(), c2.grid) < TOL32
     pred = P.degrid(d_gcf, torch.tensor(c2.grid, dtype=torch.complex64, device="cuda"))
     assert rel_l2(pred.cpu().numpy(), c2.pred) < TOL32
-    assert P.device_status() == (0, int(tile % 2 == 0))
+    # every support is even: split rows by default; the TMA form on even tiles
+    from rc_gb300 import lib
+
+    assert P.device_status() == (0, lib.STAGE_SPLIT)
+    P.set_stage(lib.STAGE_TMA)
+    pred_t = P.degrid(d_gcf, torch.tensor(c2.grid, dtype=torch.complex64, device="cuda"))
+    assert rel_l2(pred_t.cpu().numpy(), c2.pred) < TOL32
+    assert P.device_status() == (0, lib.STAGE_TMA if tile % 2 == 0 else lib.STAGE_ROWS)
+    P.set_stage(lib.STAGE_AUTO)
     lhs, rhs = _adjoint(P, ob, d_gcf, seed=tile)
     assert abs(lhs - rhs) <= TOL32 * abs(lhs)
 
