@@ -20,6 +20,11 @@ goes through checks that do not depend on size:
 - the adjoint identity holds;
 - the oracle itself runs on a 1 M-visibility sample on the full grid, with
   every support up to 128.
+
+Config 1 (516,096 visibilities, 2048^2) goes through the reference's buffer_t
+symbols against the oracle.  Config 3 (73 grids, 31.8 M visibilities) runs in
+one batched launch per direction against the FP64 pair and, for two members,
+the oracle.
 """
 import os
 from types import SimpleNamespace
@@ -283,3 +288,90 @@ def test_c5_sample_matches_the_oracle_on_the_full_grid(c5):
     assert rel_l2(grid32.cpu().numpy(), exp) < TOL32
     assert rel_l2(P.degrid(d_gcf32, d_exp.to(torch.complex64)).cpu().numpy(), exp_pred) < TOL32
     assert P.device_status()[0] == 0
+
+
+# ---------------------------------------------------------------- config 1, reference ABI
+@pytest.mark.parametrize("scatter,degrid", [("kern_scatter_gpu1", "kern_degrid_gpu1"),
+                                            ("kern_scatter", "kern_degrid"),
+                                            ("nvGridder", "kern_degrid_gpu1")])
+def test_c1_whole_observation_through_the_reference_abi(scatter, degrid):
+    """Config 1 (516,096 visibilities, 2048^2 complex128 grid, the 7x7 PSWF in
+    S = 8) through the reference's host buffer_t symbols, against the oracle's
+    restatement of kern_scatter / kern_degrid: within relative L2 1e-12."""
+    from rc_gb300 import compat
+    from rc_gb300 import gcf as G
+    from rc_gb300 import synth
+
+    ob = synth.config("c1")
+    assert ob.n == 516_096 and ob.grid_size == 2048
+    vis5 = ob.vis5()
+    gcf = G.pswf_uv_gcf(8, 7)
+    grid = np.zeros((ob.grid_size, ob.grid_size), np.complex128)
+    assert compat.call_scatter(scatter, ob.scale, ob.grid_size, 8, vis5, gcf, grid) == 0
+    exp = np.zeros_like(grid)
+    O.scatter(ob.scale, ob.grid_size, 8, vis5, gcf, exp)
+    assert np.abs(exp).max() > 0
+    assert rel_l2(grid, exp) < TOL64
+    out = np.zeros_like(vis5)
+    assert compat.call_degrid(degrid, ob.scale, ob.grid_size, 8, gcf, exp, vis5, out) == 0
+    ref = O.degrid(ob.scale, ob.grid_size, 8, gcf, exp, vis5)
+    assert np.array_equal(out[:, :3], vis5[:, :3])
+    assert rel_l2(out[:, 3:], ref[:, 3:]) < TOL64
+
+
+# ---------------------------------------------------------------- config 3, one batched launch
+def test_c3_batched_launch_at_full_size():
+    """Config 3 (73 grids of 1024^2-4096^2, 31.8 M visibilities, 48 shared
+    w-planes with supports 8-96) in one persistent launch per direction: the
+    FP32 pair within relative L2 1e-5 of the plain FP64 pair on every member,
+    and two members (a 1024^2 channel grid and a 4096^2 facet) against the
+    oracle itself."""
+    import torch
+
+    from rc_gb300 import gcf as Gm
+    from rc_gb300 import synth
+    from rc_gb300.engine import Batch
+    from rc_gb300.gcf import layout
+
+    members, scale, supports, w_planes, wlo, whi = synth.config3()
+    assert len(members) == 73 and sum(m.n for m in members) > 31_000_000
+    smax = int(supports.max())
+    tp = Gm.pswf_taper(smax)
+    g64, g32, offs = Gm.generate(w_planes, supports, smax, scale / 2, taper=tp)
+    uvws = [torch.tensor(m.uvw, device="cuda") for m in members]
+    B = Batch([dict(uvw=u, scale=scale, grid_size=m.grid_size,
+                    grid_shape=(m.grid_size, m.grid_size), supports=supports, gcf_offsets=offs,
+                    w_range=(wlo, whi)) for u, m in zip(uvws, members)],
+              tile=24, threads=256, period_cap=32)
+    vis64 = [torch.tensor(m.vis, dtype=torch.complex128, device="cuda") for m in members]
+    grids64 = [torch.zeros((m.grid_size, m.grid_size), dtype=torch.complex128, device="cuda")
+               for m in members]
+    B.grid64(vis64, g64, grids64)
+    preds64 = [torch.empty(m.n, dtype=torch.complex128, device="cuda") for m in members]
+    B.degrid64(g64, grids64, preds64)
+    grids = [torch.zeros((m.grid_size, m.grid_size), dtype=torch.complex64, device="cuda")
+             for m in members]
+    B.grid([v.to(torch.complex64) for v in vis64], g32, grids)
+    preds = B.degrid(g32, [g.to(torch.complex64) for g in grids64])
+    torch.cuda.synchronize()
+
+    def rel(a, b):
+        return float(torch.linalg.vector_norm(a.to(torch.complex128) - b) /
+                     torch.linalg.vector_norm(b))
+
+    for k in range(len(members)):
+        assert rel(grids[k], grids64[k]) < TOL32, k
+        assert rel(preds[k], preds64[k]) < TOL32, k
+    # the oracle on two whole members
+    offs_np, _ = layout(supports)
+    gcf_np = g64.cpu().numpy()
+    for k in (0, len(members) - 1):
+        m = members[k]
+        plane = O.wbin(m.uvw, wlo, whi, len(supports))
+        exp = np.zeros((m.grid_size, m.grid_size), np.complex128)
+        O.scatter_planes(scale, m.grid_size, smax, m.uvw, m.vis, plane, supports, gcf_np, offs_np,
+                         exp)
+        assert np.abs(exp).max() > 0
+        assert rel_l2(grids64[k].cpu().numpy(), exp) < TOL64, k
+        assert rel_l2(grids[k].cpu().numpy(), exp) < TOL32, k
+    B.close()
