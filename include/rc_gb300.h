@@ -362,6 +362,17 @@ int gb_image_to_grid_f64(const double *d_image, const double *d_taper, int32_t n
 int gb_grid_to_image_f64(const double *d_grid, const double *d_taper, int32_t n, double *d_work,
                          double *d_image, void *stream);
 
+/* The reference's FFT kernels on host buffers, same symbols and arguments:
+ * kern_fft(image (n,n) doubles, grid (2,n,n) doubles) and kern_ifft(grid,
+ * image), n in {1024, 2048, 3072, 4096, 6144, 8192}.  replaces
+ * MS6/kernel/cpu/gridding/fft1.cpp:29-57 (dispatch, size check) and the Halide
+ * pipelines of fft.cpp:546-677; the exact transforms are stated in
+ * rc_gb300/csrc/gb_imaging.cu.  Returns GB_ERR_FFT_SIZE for mismatched or
+ * unsupported sizes, GB_ERR_ARG for a malformed buffer.  Synchronous. */
+#define GB_ERR_FFT_SIZE (-666) /* MS6/kernel/cpu/gridding/fft1.cpp:38,52 */
+int kern_fft(buffer_t *image, buffer_t *uvg_herm);
+int kern_ifft(buffer_t *uvg, buffer_t *img_shifted);
+
 /* GCF choice for a w-region [w0, w1] among precomputed GCFs of nominal w
  * w_files[i]: the largest w_files[i] <= max(|w0|, |w1|) (the last of equal
  * ones), and whether to conjugate it (w0 < -w1: a mostly negative-w region).

@@ -14,6 +14,8 @@ Contents
     (MS4/kernel/cpu/fft/fft_dyn_padded.cpp:76-103: fftshift, unnormalised
     exp(+2*pi*i) DFT, fftshift) written as numpy's ifft2 times N^2;
   * binsizer(): the w-range rule of MS6/programs/Kernel/Binning.hs:51-60;
+  * kern_fft() / kern_ifft(): the reference's Halide FFT kernels
+    (MS6/kernel/cpu/gridding/fft.cpp:546-662) with exact twiddles;
   * ms4_* wrappers of the reference's own compiled MS4 gridder/degridder
     (oracle/_ref, built from the reference sources by `make -C oracle ref`),
     used to pin the restatement where the two index conventions coincide.
@@ -345,6 +347,50 @@ def hogbom_reference(gain, threshold, psf, res, model=None, cycles=12):
         res = res - (gain * val / pval) * shifted
         model[min(max(py, 0), ny - 1), min(max(px, 0), nx - 1)] += gain * val
     return model, res
+
+
+# ---------------------------------------------------------------- kern_fft / kern_ifft
+# The reference's Halide FFT kernels (MS6/kernel/cpu/gridding/fft.cpp) restated
+# with numpy's exact transforms.  Parity unpinned: the Halide generator cannot
+# run here, and its twiddle angles are built from float(2 pi) and
+# float(sqrt(2)/2) (fft.cpp:120, 126, 204-205, 229), about 1e-8 (relative) from
+# these exact transforms.  Arrays are [y][x] (image) and [v][u] (grid).
+
+def kern_fft(img):
+    """fftKernel (fft.cpp:607-662): the image rotated by half its size
+    (repeat_image, :617-619), its forward DFT kept for rows v <= n/2 (the
+    half spectrum of fft2d_r2c, :367-428, zero beyond: :634), then
+    out(u,v) = (B(u-h, v-h) + conj(B(h-u-1, h-v-1))) / n  (:635-638)."""
+    img = np.asarray(img, np.float64)
+    n = img.shape[0]
+    h = n // 2
+    F = np.fft.fft2(np.roll(img, (h, h), axis=(0, 1)))
+    F[h + 1:, :] = 0
+    v = np.arange(n)[:, None]
+    u = np.arange(n)[None, :]
+    return (F[(v - h) % n, (u - h) % n] + np.conj(F[(h - v - 1) % n, (h - u - 1) % n])) / n
+
+
+def kern_ifft(g):
+    """ifftKernel (fft.cpp:546-589): the grid "hermitised" about
+    (n-1-u, n-1-v) (:557-558), rotated by half (:561-563), fft2d_c2r
+    (:430-509: the inverse DFT along u of rows 0..n/2, the other rows by
+    conjugate symmetry, two real columns x and x+n/2 packed into one complex
+    inverse DFT along v), rotated back and divided by n (:572-573)."""
+    g = np.asarray(g, np.complex128)
+    n = g.shape[0]
+    h = n // 2
+    herm = (g + np.conj(g[::-1, ::-1])) / 2
+    S = np.roll(herm, (-h, -h), axis=(0, 1))
+    D = n * np.fft.ifft(S[:h + 1], axis=1)
+    X = np.empty((n, n), np.complex128)
+    X[:h] = D[:h]
+    X[h:] = np.conj(D[n - np.arange(h, n)])
+    T = n * np.fft.ifft(X, axis=0)
+    image = np.empty((n, n))
+    image[:, :h] = T[:, :h].real - T[:, h:].imag
+    image[:, h:] = T[:, :h].imag + T[:, h:].real
+    return np.roll(image, (-h, -h), axis=(0, 1)) / n
 
 
 # ---------------------------------------------------------------- detile / rotate

@@ -54,6 +54,27 @@ def grid_buf(grid: np.ndarray, min_x=0, min_y=0):
     return buf(d, [(2, 1), (W, 2), (H, 2 * W)], (0, min_x, min_y, 0))
 
 
+def image_buf(img: np.ndarray):
+    """(n, n) doubles, [y][x]: dims (n, n), strides (1, n) (the reference's
+    real image buffers, MS6/kernel/cpu/gridding/fft.cpp:609-611)."""
+    assert img.flags.c_contiguous and img.ndim == 2
+    return buf(img, [(img.shape[1], 1), (img.shape[0], img.shape[1])])
+
+
+def call_fft(image, grid):
+    """kern_fft: real image (n, n) -> complex grid (n, n) in place."""
+    L = _lib.load()
+    ib, gb = image_buf(image), grid_buf(grid)
+    return L.kern_fft(C.byref(ib), C.byref(gb))
+
+
+def call_ifft(grid, image):
+    """kern_ifft: complex grid (n, n) -> real image (n, n) in place."""
+    L = _lib.load()
+    gb, ib = grid_buf(grid), image_buf(image)
+    return L.kern_ifft(C.byref(gb), C.byref(ib))
+
+
 def call_scatter(name, scale, grid_size, margin, vis5, gcf, grid, min_x=0, min_y=0):
     L = _lib.load()
     vb, gb, ub = vis_buf(vis5), gcf_buf(gcf), grid_buf(grid, min_x, min_y)

@@ -184,9 +184,226 @@ static int grid_to_image(const typename Cx<R>::T* g, const R* t, int n, typename
   return GB_OK;
 }
 
+// ---------------------------------------------------------------- kern_fft / kern_ifft
+// The reference's Halide FFT kernels on host buffers (MS6/kernel/cpu/gridding/
+// fft.cpp:546-677, bound by fft1.cpp:29-57), restated on cuFFT in FP64.  For an
+// n x n grid g (complex) and image x (real), n in {1024, 2048, 3072, 4096,
+// 6144, 8192}, indices taken mod n, h = n / 2:
+//
+// kern_ifft (fft.cpp:546-589):
+//   H(u,v)  = (g(u,v) + conj(g(n-1-u, n-1-v))) / 2          the "hermitised" grid
+//   S(u,v)  = H(u+h, v+h)
+//   D(x,v)  = sum_u S(u,v) e^{+2 pi i u x/n}                  rows v = 0..h only
+//   X(x,v)  = D(x,v) for v < h, conj(D(x, n-v)) for v >= h    (fft2d_c2r, :430-509)
+//   T_x(y)  = sum_v X(x,v) e^{+2 pi i v y/n}
+//   I(x,y)  = Re T_x(y) - Im T_{x+h}(y)  (x < h),  Im T_{x-h}(y) + Re T_x(y)  (x >= h)
+//             (two real columns packed into one complex transform; where X's rows 0
+//             and h are not real, the imaginary parts cross between the two columns)
+//   out(x,y) = I(x+h, y+h) / n
+// kern_fft (fft.cpp:607-662):
+//   F(u,v)  = sum_{x,y} x(x-h, y-h) e^{-2 pi i (u x + v y)/n}, kept for rows v <= h
+//             (fft2d_r2c's half spectrum, zero elsewhere): B
+//   out(u,v) = (B(u-h, v-h) + conj(B(h-u-1, h-v-1))) / n
+// The reference builds its twiddle angles from float(2 pi) and float(sqrt(2)/2),
+// so it sits about 1e-8 (relative) from these exact transforms.
+constexpr int kFftSizeError = -666;  // fft1.cpp:38, 52
+
+__global__ void k_ifft_prep(const double2* __restrict__ g, int n, double2* __restrict__ a) {
+  const int h = n / 2;
+  const int64_t total = (int64_t)(h + 1) * n;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int v = (int)(i / n), u = (int)(i - (int64_t)v * n);
+    const int ua = half_shift(u, n), vb = half_shift(v, n);
+    const double2 p = g[(int64_t)vb * n + ua];
+    const double2 m = g[(int64_t)(n - 1 - vb) * n + (n - 1 - ua)];
+    a[i] = make_double2((p.x + m.x) / 2, (p.y - m.y) / 2);
+  }
+}
+
+__global__ void k_ifft_complete(const double2* __restrict__ a, int n, double2* __restrict__ b) {
+  const int h = n / 2;
+  const int64_t total = (int64_t)n * n;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int v = (int)(i / n), x = (int)(i - (int64_t)v * n);
+    if (v < h) {
+      b[i] = a[i];
+    } else {
+      const double2 d = a[(int64_t)(n - v) * n + x];
+      b[i] = make_double2(d.x, -d.y);
+    }
+  }
+}
+
+__global__ void k_ifft_out(const double2* __restrict__ t, int n, double* __restrict__ out) {
+  const int h = n / 2;
+  const int64_t total = (int64_t)n * n;
+  const double rn = 1.0 / n;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int y = (int)(i / n), x = (int)(i - (int64_t)y * n);
+    const int sx = half_shift(x, n), sy = half_shift(y, n);
+    const double2* row = t + (int64_t)sy * n;
+    const double val = sx < h ? row[sx].x - row[sx + h].y : row[sx - h].y + row[sx].x;
+    out[i] = val * rn;
+  }
+}
+
+__global__ void k_fft_prep(const double* __restrict__ img, int n, double2* __restrict__ z) {
+  const int64_t total = (int64_t)n * n;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int v = (int)(i / n), u = (int)(i - (int64_t)v * n);
+    z[i] = make_double2(img[(int64_t)half_shift(v, n) * n + half_shift(u, n)], 0.0);
+  }
+}
+
+__global__ void k_fft_out(const double2* __restrict__ f, int n, double2* __restrict__ out) {
+  const int h = n / 2;
+  const int64_t total = (int64_t)n * n;
+  const double rn = 1.0 / n;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int v = (int)(i / n), u = (int)(i - (int64_t)v * n);
+    const int a1 = half_shift(u, n), b1 = half_shift(v, n);  // u - h, v - h (mod n)
+    const int a2 = h - 1 - u < 0 ? h - 1 - u + n : h - 1 - u;
+    const int b2 = h - 1 - v < 0 ? h - 1 - v + n : h - 1 - v;
+    const double2 t1 = b1 <= h ? f[(int64_t)b1 * n + a1] : make_double2(0.0, 0.0);
+    const double2 t2 = b2 <= h ? f[(int64_t)b2 * n + a2] : make_double2(0.0, 0.0);
+    out[i] = make_double2((t1.x + t2.x) * rn, (t1.y - t2.y) * rn);
+  }
+}
+
+// Batched 1-D double-complex plans (rows: stride 1, dist n; columns: stride n,
+// dist 1), one per (device, n, batch, layout), created on first use.
+static int plan_1d(int n, int batch, bool columns, cufftHandle* out) {
+  static std::mutex mu;
+  static std::map<std::tuple<int, int, int, int>, cufftHandle> plans;
+  int dev = 0;
+  GB_CUDA_TRY(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(mu);
+  auto key = std::make_tuple(dev, n, batch, columns ? 1 : 0);
+  auto it = plans.find(key);
+  if (it != plans.end()) {
+    *out = it->second;
+    return GB_OK;
+  }
+  cufftHandle hdl;
+  int len = n, emb = n;
+  const int stride = columns ? n : 1, dist = columns ? 1 : n;
+  const cufftResult r = cufftPlanMany(&hdl, 1, &len, &emb, stride, dist, &emb, stride, dist,
+                                      CUFFT_Z2Z, batch);
+  if (r != CUFFT_SUCCESS) {
+    gb_set_error(GB_ERR_CUDA, "cufftPlanMany(%d x %d): error %d", n, batch, (int)r);
+    return GB_ERR_CUDA;
+  }
+  plans[key] = hdl;
+  *out = hdl;
+  return GB_OK;
+}
+
+static int exec_1d(double2* buf, int n, int batch, bool columns, cudaStream_t s) {
+  cufftHandle hdl;
+  int rc = plan_1d(n, batch, columns, &hdl);
+  if (rc) return rc;
+  std::lock_guard<std::mutex> lk(g_exec_mu);
+  cufftResult r = cufftSetStream(hdl, s);
+  if (r == CUFFT_SUCCESS)
+    r = cufftExecZ2Z(hdl, (cufftDoubleComplex*)buf, (cufftDoubleComplex*)buf, CUFFT_INVERSE);
+  if (r != CUFFT_SUCCESS) {
+    gb_set_error(GB_ERR_CUDA, "cuFFT exec 1-D (n=%d): error %d", n, (int)r);
+    return GB_ERR_CUDA;
+  }
+  return GB_OK;
+}
+
+// fft1.cpp:3-11 (checkSize) plus the layouts the Halide pipelines require:
+// image (n, n) doubles with unit stride, grid (2, n, n) doubles with strides
+// (1, 2, >= 2n), all mins 0.  Returns n, kFftSizeError for a size the
+// reference does not provide, or GB_ERR_ARG for a malformed buffer.
+static int fft_size(const buffer_t* img, const buffer_t* uvg, const char* who) {
+  if (!img || !uvg || !img->host || !uvg->host || img->elem_size != 8 || uvg->elem_size != 8 ||
+      img->stride[0] != 1 || uvg->extent[0] != 2 || uvg->stride[0] != 1 || uvg->stride[1] != 2 ||
+      img->min[0] || img->min[1] || uvg->min[0] || uvg->min[1] || uvg->min[2]) {
+    gb_set_error(GB_ERR_ARG, "%s: image must be (n,n) doubles with unit stride and the grid "
+                             "(2,n,n) doubles with strides (1,2,>=2n), mins 0", who);
+    return GB_ERR_ARG;
+  }
+  const int n = img->extent[0];
+  if (img->extent[1] != n || uvg->extent[1] != n || uvg->extent[2] != n) {
+    gb_set_error(kFftSizeError, "%s: image and grid must both be n x n", who);
+    return kFftSizeError;
+  }
+  if (n != 1024 && n != 2048 && n != 3072 && n != 4096 && n != 6144 && n != 8192) {
+    gb_set_error(kFftSizeError, "%s: n = %d is not one of the reference's sizes", who, n);
+    return kFftSizeError;
+  }
+  if (img->stride[1] < n || uvg->stride[2] < 2 * n || (uvg->stride[2] & 1)) {
+    gb_set_error(GB_ERR_ARG, "%s: row strides too small", who);
+    return GB_ERR_ARG;
+  }
+  return n;
+}
+
 }  // namespace gb
 
 using namespace gb;
+
+extern "C" int kern_ifft(buffer_t* uvg, buffer_t* img) {
+  const int n = fft_size(img, uvg, "kern_ifft");
+  if (n < 0) return n;
+  int rc;
+  cudaStream_t s;
+  if ((rc = stage_stream(&s))) return rc;
+  const size_t cells = (size_t)n * n;
+  void *d0, *d1;
+  if ((rc = stage_buffer(0, cells * 16, &d0)) || (rc = stage_buffer(1, cells * 16, &d1)))
+    return rc;
+  double2* g = (double2*)d0;
+  double2* a = (double2*)d1;
+  GB_CUDA_TRY(cudaMemcpy2DAsync(g, (size_t)n * 16, uvg->host, (size_t)uvg->stride[2] * 8,
+                                (size_t)n * 16, n, cudaMemcpyHostToDevice, s));
+  k_ifft_prep<<<blocks_nn((int64_t)(n / 2 + 1) * n), 256, 0, s>>>(g, n, a);
+  GB_CUDA_TRY(cudaGetLastError());
+  if ((rc = exec_1d(a, n, n / 2 + 1, false, s))) return rc;
+  k_ifft_complete<<<blocks_nn((int64_t)cells), 256, 0, s>>>(a, n, g);
+  GB_CUDA_TRY(cudaGetLastError());
+  if ((rc = exec_1d(g, n, n, true, s))) return rc;
+  double* out = (double*)d1;
+  k_ifft_out<<<blocks_nn((int64_t)cells), 256, 0, s>>>(g, n, out);
+  GB_CUDA_TRY(cudaGetLastError());
+  GB_CUDA_TRY(cudaMemcpy2DAsync(img->host, (size_t)img->stride[1] * 8, out, (size_t)n * 8,
+                                (size_t)n * 8, n, cudaMemcpyDeviceToHost, s));
+  GB_CUDA_TRY(cudaStreamSynchronize(s));
+  return GB_OK;
+}
+
+extern "C" int kern_fft(buffer_t* img, buffer_t* uvg) {
+  const int n = fft_size(img, uvg, "kern_fft");
+  if (n < 0) return n;
+  int rc;
+  cudaStream_t s;
+  if ((rc = stage_stream(&s))) return rc;
+  const size_t cells = (size_t)n * n;
+  void *d0, *d1;
+  if ((rc = stage_buffer(0, cells * 16, &d0)) || (rc = stage_buffer(1, cells * 16, &d1)))
+    return rc;
+  double* x = (double*)d1;
+  double2* z = (double2*)d0;
+  GB_CUDA_TRY(cudaMemcpy2DAsync(x, (size_t)n * 8, img->host, (size_t)img->stride[1] * 8,
+                                (size_t)n * 8, n, cudaMemcpyHostToDevice, s));
+  k_fft_prep<<<blocks_nn((int64_t)cells), 256, 0, s>>>(x, n, z);
+  GB_CUDA_TRY(cudaGetLastError());
+  if ((rc = exec_fft<double>(z, n, CUFFT_FORWARD, s))) return rc;
+  double2* out = (double2*)d1;
+  k_fft_out<<<blocks_nn((int64_t)cells), 256, 0, s>>>(z, n, out);
+  GB_CUDA_TRY(cudaGetLastError());
+  GB_CUDA_TRY(cudaMemcpy2DAsync(uvg->host, (size_t)uvg->stride[2] * 8, out, (size_t)n * 16,
+                                (size_t)n * 16, n, cudaMemcpyDeviceToHost, s));
+  GB_CUDA_TRY(cudaStreamSynchronize(s));
+  return GB_OK;
+}
 
 extern "C" int gb_image_to_grid_f32(const float* d_image, const float* d_taper, int32_t n,
                                     float* d_grid, void* stream) {

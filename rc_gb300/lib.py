@@ -22,6 +22,7 @@ ERR_CUDA = -1002
 ERR_TIMEOUT = -1003
 ERR_NOMEM = -1004
 ERR_CAPACITY = -1005
+ERR_FFT_SIZE = -666
 # staging forms of FP32 degridding (gb_plan_set_stage)
 STAGE_AUTO, STAGE_SPLIT, STAGE_TMA, STAGE_ROWS = -1, 0, 1, 2
 
@@ -131,6 +132,8 @@ SIGNATURES = {
     "gb_plan_stats": (C.c_int, [_VP, C.POINTER(C.c_int64)]),
     "gb_plan_device_status": (C.c_int, [_VP, C.POINTER(C.c_int32), _VP]),
     "gb_plan_set_stage": (C.c_int, [_VP, C.c_int32]),
+    "kern_fft": (C.c_int, [_VP, _VP]),
+    "kern_ifft": (C.c_int, [_VP, _VP]),
     "gb_plan_export_index": (C.c_int, [_VP, _VP, _VP]),
     "gb_grid_f32": (C.c_int, [_VP, _VP, _VP, _VP, _VP]),
     "gb_degrid_f32": (C.c_int, [_VP, _VP, _VP, _VP, C.c_int32, _VP]),
