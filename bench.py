@@ -430,40 +430,77 @@ def our_arm(args):
         except Exception:
             traffic = None
 
-    # end to end through the public API: pinned host vis + model grid in,
-    # grid + predictions out, every step.  Gridding needs only the
-    # visibilities and degridding only the model grid, so each runs on its own
-    # stream with its copies: the model upload overlaps gridding and the grid
-    # download overlaps degridding.  Events on the launching stream bracket
-    # every copy and both kernels.
+    # end to end through the public API: every step uploads its visibilities
+    # and model grid from pinned host memory and downloads its grid and
+    # predictions, inside the timed region.  Device and host buffers are
+    # double-buffered and the copies run on their own streams, so step i+1's
+    # uploads overlap step i's degridding, step i's grid download overlaps its
+    # degridding and its prediction download overlaps step i+1's gridding: in
+    # steady state a step costs its kernels plus what the copies cannot hide.
+    # The per-step working set (about 300 MB) is larger than L2.
     h_vis = torch.tensor(ob.vis, dtype=torch.complex64).pin_memory()
     h_model = model32.cpu().pin_memory()
-    h_grid = torch.empty((G, G), dtype=torch.complex64).pin_memory()
-    h_pred = torch.empty(ob.n, dtype=torch.complex64).pin_memory()
-    d_vis_e = torch.empty_like(vis32)
-    d_model_e = torch.empty_like(model32)
-    s_deg = torch.cuda.Stream(dev)
-    e2e = []
-    for i in range(0 if args.quick else args.warmup + args.steps):
-        flush.fill_(float(i))
-        ev[0].record(s)
-        s_deg.wait_event(ev[0])
-        d_vis_e.copy_(h_vis, non_blocking=True)
-        grid.zero_()
-        plan.grid(d_vis_e, g32, grid)
-        h_grid.copy_(grid, non_blocking=True)
-        with torch.cuda.stream(s_deg):
-            d_model_e.copy_(h_model, non_blocking=True)
-            plan.degrid(g32, d_model_e, out=pred)
-            h_pred.copy_(pred, non_blocking=True)
-        s.wait_stream(s_deg)
-        ev[1].record(s)
-        ev[1].synchronize()
-        if i >= args.warmup:
-            e2e.append(ev[0].elapsed_time(ev[1]))
-    e2e_mvis = world * ob.n / (float(np.mean(e2e)) * 1e-3) / 1e6 if e2e else float("nan")
+    h_grid = [torch.empty((G, G), dtype=torch.complex64).pin_memory() for _ in range(2)]
+    h_pred = [torch.empty(ob.n, dtype=torch.complex64).pin_memory() for _ in range(2)]
+    d_vis_e = [torch.empty_like(vis32) for _ in range(2)]
+    d_model_e = [torch.empty_like(model32) for _ in range(2)]
+    d_grid_e = [grid, torch.empty_like(grid)]
+    d_pred_e = [pred, torch.empty_like(pred)]
+    s_up, s_down = torch.cuda.Stream(dev), torch.cuda.Stream(dev)
+
+    def pipeline(k, start):
+        mk = [[torch.cuda.Event() for _ in range(k)] for _ in range(6)]
+        vis_up, model_up, grid_done, deg_done, grid_down, pred_down = mk
+        s_up.wait_event(start)
+        for i in range(k):
+            b = i % 2
+            with torch.cuda.stream(s_up):
+                if i >= 2:
+                    s_up.wait_event(grid_done[i - 2])
+                d_vis_e[b].copy_(h_vis, non_blocking=True)
+                vis_up[i].record(s_up)
+                if i >= 2:
+                    s_up.wait_event(deg_done[i - 2])
+                d_model_e[b].copy_(h_model, non_blocking=True)
+                model_up[i].record(s_up)
+            s.wait_event(vis_up[i])
+            if i >= 2:
+                s.wait_event(grid_down[i - 2])
+            d_grid_e[b].zero_()
+            plan.grid(d_vis_e[b], g32, d_grid_e[b])
+            grid_done[i].record(s)
+            s.wait_event(model_up[i])
+            if i >= 2:
+                s.wait_event(pred_down[i - 2])
+            plan.degrid(g32, d_model_e[b], out=d_pred_e[b])
+            deg_done[i].record(s)
+            with torch.cuda.stream(s_down):
+                s_down.wait_event(grid_done[i])
+                h_grid[b].copy_(d_grid_e[b], non_blocking=True)
+                grid_down[i].record(s_down)
+                s_down.wait_event(deg_done[i])
+                h_pred[b].copy_(d_pred_e[b], non_blocking=True)
+                pred_down[i].record(s_down)
+        s.wait_stream(s_up)
+        s.wait_stream(s_down)
+
+    e2e_ms = None
+    if not args.quick:
+        st0 = torch.cuda.Event()
+        st0.record(s)
+        pipeline(args.warmup, st0)
+        torch.cuda.synchronize()
+        t0e, t1e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0e.record(s)
+        pipeline(args.steps, t0e)
+        t1e.record(s)
+        t1e.synchronize()
+        e2e_ms = t0e.elapsed_time(t1e) / args.steps
+        # the last step's results are the step's own
+        assert torch.equal(h_pred[(args.steps - 1) % 2], d_pred_e[(args.steps - 1) % 2].cpu())
+    e2e_mvis = world * ob.n / (e2e_ms * 1e-3) / 1e6 if e2e_ms else float("nan")
     h2d = h_vis.numel() * 8 + h_model.numel() * 8
-    d2h = h_grid.numel() * 8 + h_pred.numel() * 8
+    d2h = h_grid[0].numel() * 8 + h_pred[0].numel() * 8
 
     # CPU baseline (rank 0, N = 1 only): the oracle port on the host cores
     cpu = None
@@ -501,11 +538,9 @@ def our_arm(args):
             "rel_l2_vs_fp64": {"grid": err_grid, "degrid": err_deg, "bar": 1e-5},
             "e2e": {"value": round(e2e_mvis, 3), "unit": "Mvis/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h,
-                    "ms_per_step": round(float(np.mean(e2e)), 3) if e2e else None,
-                    # the copies cross the host link, which other jobs on the
-                    # machine may share: the spread shows a disturbed run
-                    "ms_median": round(float(np.median(e2e)), 3) if e2e else None,
-                    "ms_max": round(float(np.max(e2e)), 3) if e2e else None},
+                    "ms_per_step": round(e2e_ms, 3) if e2e_ms else None,
+                    "timing": "K steps pipelined (double-buffered, copies on their own "
+                              "streams) between two events, / K"},
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
             "gpu_launches": 2 * args.steps,
