@@ -484,7 +484,7 @@ def our_arm(args):
         s.wait_stream(s_up)
         s.wait_stream(s_down)
 
-    e2e_ms = None
+    e2e_ms = e2e_lat = None
     if not args.quick:
         st0 = torch.cuda.Event()
         st0.record(s)
@@ -498,6 +498,17 @@ def our_arm(args):
         e2e_ms = t0e.elapsed_time(t1e) / args.steps
         # the last step's results are the step's own
         assert torch.equal(h_pred[(args.steps - 1) % 2], d_pred_e[(args.steps - 1) % 2].cpu())
+        # latency of one step on its own (no neighbour to overlap with): the
+        # same copies and kernels, each step bracketed by events and waited on
+        lat = []
+        for i in range(args.warmup + args.steps):
+            t0e.record(s)
+            pipeline(1, t0e)
+            t1e.record(s)
+            t1e.synchronize()
+            if i >= args.warmup:
+                lat.append(t0e.elapsed_time(t1e))
+        e2e_lat = float(np.median(lat))
     e2e_mvis = world * ob.n / (e2e_ms * 1e-3) / 1e6 if e2e_ms else float("nan")
     h2d = h_vis.numel() * 8 + h_model.numel() * 8
     d2h = h_grid[0].numel() * 8 + h_pred[0].numel() * 8
@@ -540,7 +551,8 @@ def our_arm(args):
                     "d2h_bytes_per_step": d2h,
                     "ms_per_step": round(e2e_ms, 3) if e2e_ms else None,
                     "timing": "K steps pipelined (double-buffered, copies on their own "
-                              "streams) between two events, / K"},
+                              "streams) between two events, / K",
+                    "single_step_latency_ms": round(e2e_lat, 3) if e2e_lat else None},
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
             "gpu_launches": 2 * args.steps,
