@@ -7,8 +7,6 @@ import os
 import re
 import subprocess
 
-import pytest
-
 from rc_gb300 import lib
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
