@@ -598,7 +598,7 @@ def our_arm_batch(args):
                       for u, m in zip(uvws, members)], **p)
 
     params = dict(tile=args.tile or 24, threads=args.threads or 256,
-                  period_cap=args.cap or 32, bundles_per_cta=4)
+                  period_cap=args.cap or 40, bundles_per_cta=4)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     B = make_batch(**params)
@@ -736,7 +736,7 @@ def our_arm_major_cycle(args):
     t0 = time.perf_counter()
     plan = Plan(uvw, scale=ob.scale, grid_size=n, grid_shape=(n, n), supports=ob.supports,
                 w_range=(ob.w_low, ob.w_high), tile=args.tile or 24, threads=args.threads or 256,
-                period_cap=args.cap or 32)
+                period_cap=args.cap or 40)
     torch.cuda.synchronize()
     plan_ms = 1e3 * (time.perf_counter() - t0)
     st = plan.stats()

@@ -128,9 +128,10 @@ typedef struct gb_geometry {
   int32_t ext_x, ext_y;
   int64_t pitch;
   int32_t n_planes;
-  int32_t tile;            /* grid tile edge of the FP32 kernels (8..128): 0 = 32 */
+  int32_t tile;            /* grid tile edge of the FP32 kernels (8..128): 0 = 24 */
   int32_t threads;         /* threads per CTA of the FP32 kernels (128, 256, 512): 0 = 256 */
-  int32_t period_cap;      /* largest footprint piece edge (8..64): 0 = 32 */
+  int32_t period_cap;      /* largest footprint piece edge (8..64, cap^2 <= 8 threads):
+                              0 = 40 (32 with 128 threads) */
   int32_t bundles_per_cta; /* work granularity: target bundles per resident CTA (1..64): 0 = 4 */
   const int32_t *supports; /* host, n_planes */
   const int64_t *gcf_offsets; /* host, n_planes */

@@ -22,13 +22,13 @@ import os
 
 import numpy as np
 
-DEFAULT = {"tile": 24, "threads": 256, "period_cap": 32, "bundles_per_cta": 4}
+DEFAULT = {"tile": 24, "threads": 256, "period_cap": 40, "bundles_per_cta": 4}
 
 CANDIDATES = [
     {"tile": t, "threads": nt, "period_cap": cap, "bundles_per_cta": b}
     for t in (16, 24, 32)
     for nt in (256, 512)
-    for cap in (24, 32)
+    for cap in (24, 32, 40)
     for b in (2, 4, 8)
 ]
 

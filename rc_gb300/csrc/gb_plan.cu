@@ -498,9 +498,12 @@ extern "C" int gb_plan_create(const gb_geometry* geo, int64_t n_vis, const doubl
     }
     smax = std::max(smax, S);
   }
-  const int T = geo->tile ? geo->tile : 32;
+  // defaults: the measured best on the benchmark workloads (tile 24 with
+  // 256 threads; pieces up to 40 x 40, so supports up to 40 stay whole and a
+  // CTA's accumulators still let three CTAs share an SM)
+  const int T = geo->tile ? geo->tile : 24;
   const int NT = geo->threads ? geo->threads : 256;
-  const int cap = geo->period_cap ? geo->period_cap : 32;
+  const int cap = geo->period_cap ? geo->period_cap : (40 * 40 <= 8 * NT ? 40 : 32);
   const int bpc = geo->bundles_per_cta ? geo->bundles_per_cta : 4;
   if (T < 8 || T > 128 || (NT != 128 && NT != 256 && NT != 512) || cap < 8 || cap > 64 ||
       cap * cap > 8 * NT || bpc < 1 || bpc > 64 || geo->ext_x > 32767 * T ||
