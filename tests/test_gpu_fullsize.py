@@ -159,8 +159,16 @@ def test_c2_plain_fp64_pair_matches_the_oracle(c2):
     grid = torch.zeros((G, G), dtype=torch.complex128, device="cuda")
     P.grid64(torch.tensor(ob.vis, dtype=torch.complex128, device="cuda"), d_gcf, grid)
     assert rel_l2(grid.cpu().numpy(), c2.grid) < TOL64
-    pred = P.degrid64(d_gcf, torch.tensor(c2.grid, device="cuda")).cpu().numpy()
+    d_grid = torch.tensor(c2.grid, device="cuda")
+    pred = P.degrid64(d_gcf, d_grid).cpu().numpy()
     assert rel_l2(pred, c2.pred) < TOL64
+    # mode 1: the reference kern_degrid product, -sum grid * gcf (no conjugate),
+    # FP64 and FP32 against the oracle on the whole observation
+    exp1 = O.degrid_planes(ob.scale, G, c2.margin, ob.uvw, c2.plane, ob.supports, c2.gcf, c2.offs,
+                           c2.grid, mode=1, nthreads=NTHREADS)
+    assert rel_l2(P.degrid64(d_gcf, d_grid, mode=1).cpu().numpy(), exp1) < TOL64
+    pred32 = P.degrid(d_gcf.to(torch.complex64), d_grid.to(torch.complex64), mode=1)
+    assert rel_l2(pred32.cpu().numpy(), exp1) < TOL32
 
 
 @pytest.mark.parametrize("tile,threads,cap", [(24, 256, 32), (25, 256, 32), (32, 512, 64)])
