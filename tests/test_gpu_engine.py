@@ -268,3 +268,54 @@ def test_fp32_repeat_is_stable():
     P.grid(d_vis, d_gcf, g1)
     P.grid(d_vis, d_gcf, g2)
     assert rel_l2(g1.cpu().numpy(), g2.cpu().numpy()) < 1e-6
+
+
+@pytest.mark.parametrize("tile,threads,cap", [(24, 0, 0), (8, 512, 64), (32, 256, 32)])
+def test_largest_supports(tile, threads, cap):
+    """Supports up to the library's limit (GB_MAX_SUPPORT = 256), odd and even,
+    cut into pieces of up to cap x cap: indices, FP32 pair and FP64 pair
+    against the oracle."""
+    torch = torch_mod()
+    c = random_case(11, n=600, G=1024, supports=(256, 255, 129, 2))
+    P = make_plan(c, tile=tile, threads=threads, cap=cap)
+    got = P.export_index().cpu().numpy()
+    exp = oracle_index(c)
+    kept = exp[:, 4] == 1
+    assert kept.sum() > 300
+    assert np.array_equal(got[:, 3:5], exp[:, 3:5])
+    assert np.array_equal(got[kept, :3], exp[kept, :3])
+    d_gcf32 = torch.tensor(c["gcf"], dtype=torch.complex64, device="cuda")
+    grid = torch.zeros((c["G"], c["G"]), dtype=torch.complex64, device="cuda")
+    P.grid(torch.tensor(c["vis"], dtype=torch.complex64, device="cuda"), d_gcf32, grid)
+    ref = oracle_grid(c)
+    assert rel_l2(grid.cpu().numpy(), ref) < TOL32
+    model = np.random.default_rng(12).standard_normal((c["G"], c["G"])) * (1 - 2j)
+    pred = P.degrid(d_gcf32, torch.tensor(model, dtype=torch.complex64, device="cuda"))
+    assert rel_l2(pred.cpu().numpy(), oracle_degrid(c, model)) < TOL32
+    g64 = torch.zeros((c["G"], c["G"]), dtype=torch.complex128, device="cuda")
+    P.grid64(torch.tensor(c["vis"], device="cuda"), torch.tensor(c["gcf"], device="cuda"), g64)
+    assert rel_l2(g64.cpu().numpy(), ref) < TOL64
+
+
+def test_single_visibility_each_plane():
+    """One visibility per plane, one of them at the last corner the bounds rule
+    keeps and one a pixel past it (the rule's extra -1 drops it): the
+    footprints land exactly where the oracle puts them."""
+    torch = torch_mod()
+    c = random_case(13, n=5, G=256, supports=(8, 31, 64, 1))
+    G = c["G"]
+    # S = 64 with margin 64: corner x0 = round(u) + G/2 - 32 is kept up to
+    # G - 64 - 1 = 191, i.e. u = 95; u = 96 gives x0 = 192, dropped
+    c["uvw"] = np.array([[0.0, 0.0, 0.0], [12.25, -7.5, 0.0], [95.0, 3.0, 0.0],
+                         [-3.0, 40.375, 0.0], [96.0, 3.0, 0.0]])
+    c["plane"] = np.array([0, 1, 2, 3, 2], np.int32)
+    P = make_plan(c)
+    exp_idx = oracle_index(c)
+    assert exp_idx[2, 0] == 191 and exp_idx[2, 4] == 1 and exp_idx[4, 4] == 0
+    got = P.export_index().cpu().numpy()
+    assert np.array_equal(got[:, 3:5], exp_idx[:, 3:5])
+    assert np.array_equal(got[:4, :3], exp_idx[:4, :3])
+    d_gcf = torch.tensor(c["gcf"], dtype=torch.complex64, device="cuda")
+    grid = torch.zeros((G, G), dtype=torch.complex64, device="cuda")
+    P.grid(torch.tensor(c["vis"], dtype=torch.complex64, device="cuda"), d_gcf, grid)
+    assert rel_l2(grid.cpu().numpy(), oracle_grid(c)) < TOL32
