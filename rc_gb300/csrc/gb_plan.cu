@@ -183,39 +183,53 @@ static int dalloc(T** p, size_t n) {
 
 void make_bundles(const std::vector<HostItem>& items, const ClassInfo* cls, int n_classes,
                   std::vector<Item>& it_out, std::vector<Bundle>& b_out) {
+  // items by (class, grid slot), each bucket in the items' own order: one
+  // counting pass (a batch has up to kMaxGrids slots)
+  int max_grid = 0;
+  for (const auto& h : items) max_grid = std::max(max_grid, h.grid);
+  const size_t ng = (size_t)max_grid + 1, nb = (size_t)n_classes * ng;
+  std::vector<size_t> first(nb + 1, 0);
+  for (const auto& h : items) first[(size_t)h.it.cls * ng + h.grid + 1]++;
+  for (size_t k = 1; k <= nb; k++) first[k] += first[k - 1];
+  std::vector<int32_t> order(items.size());
+  {
+    std::vector<size_t> next(first.begin(), first.end() - 1);
+    for (size_t i = 0; i < items.size(); i++)
+      order[next[(size_t)items[i].it.cls * ng + items[i].grid]++] = (int32_t)i;
+  }
+  // within a bucket, longest first; groups of G items form a bundle
   struct HB {
     Bundle b;
     double cost;
   };
   std::vector<HB> bundles;
-  int max_grid = 0;
-  for (const auto& h : items) max_grid = std::max(max_grid, h.grid);
   it_out.clear();
+  it_out.reserve(items.size());
+  const auto longer = [&](int32_t a, int32_t b) { return items[a].cost > items[b].cost; };
   for (int c = 0; c < n_classes; c++) {
-    for (int g = 0; g <= max_grid; g++) {
-      std::vector<HostItem> ci;
-      for (const auto& h : items)
-        if (h.it.cls == c && h.grid == g) ci.push_back(h);
-      if (ci.empty()) continue;
-      std::stable_sort(ci.begin(), ci.end(),
-                       [](const HostItem& a, const HostItem& b) { return a.cost > b.cost; });
-      const int G = cls[c].G;
-      for (size_t i = 0; i < ci.size(); i += G) {
+    const int G = cls[c].G;
+    for (size_t g = 0; g < ng; g++) {
+      const size_t k = (size_t)c * ng + g;
+      if (first[k] == first[k + 1]) continue;
+      std::stable_sort(order.begin() + first[k], order.begin() + first[k + 1], longer);
+      for (size_t i = first[k]; i < first[k + 1]; i += G) {
         HB hb;
         hb.b.first_item = (int32_t)it_out.size();
-        hb.b.n_items = (int16_t)std::min<size_t>(G, ci.size() - i);
+        hb.b.n_items = (int16_t)std::min<size_t>(G, first[k + 1] - i);
         hb.b.cls = (int16_t)c;
-        hb.b.grid = g;
+        hb.b.grid = (int32_t)g;
         hb.b.pad = 0;
-        hb.cost = ci[i].cost;
-        for (int k = 0; k < hb.b.n_items; k++) it_out.push_back(ci[i + k].it);
+        hb.cost = items[order[i]].cost;
+        for (int m = 0; m < hb.b.n_items; m++) it_out.push_back(items[order[i + m]].it);
         bundles.push_back(hb);
       }
     }
   }
+  // all bundles, longest first
   std::stable_sort(bundles.begin(), bundles.end(),
                    [](const HB& a, const HB& b) { return a.cost > b.cost; });
   b_out.clear();
+  b_out.reserve(bundles.size());
   for (auto& hb : bundles) b_out.push_back(hb.b);
 }
 
@@ -367,10 +381,11 @@ static int build_plan(gb_plan* P, const gb_geometry* geo, int64_t n_vis, const d
   // cost model, in thread-group steps: a piece of period P costs ceil(P^2/L)
   // tap rounds plus one for its record; an item adds zeroing + flush of its
   // A x A accumulator.
-  auto rec_cost = [&](int r) {
+  std::vector<double> rec_cost(nper);
+  for (int r = 0; r < nper; r++) {
     const int L = P->cls[rank_cls[r]].L;
-    return (double)((periods[r] * periods[r] + L - 1) / L + 1);
-  };
+    rec_cost[r] = (double)((periods[r] * periods[r] + L - 1) / L + 1);
+  }
   auto fixed_cost = [&](int c) {
     const ClassInfo& ci = P->cls[c];
     return (double)(2 * ((ci.A * ci.A + ci.L - 1) / ci.L));
@@ -379,10 +394,16 @@ static int build_plan(gb_plan* P, const gb_geometry* geo, int64_t n_vis, const d
   for (int64_t k = 0; k < nkeys; k++)
     if (hist[k]) {
       const int r = (int)(k % nper);
-      total_cta += hist[k] * rec_cost(r) / P->cls[rank_cls[r]].G;
+      total_cta += hist[k] * rec_cost[r] / P->cls[rank_cls[r]].G;
     }
   const int ctas = std::max(1, sm_count() * std::max(1, P->ctas_per_sm_grid));
   const double tau = total_cta / ((double)P->bpc * ctas);
+  // a class's periods are consecutive ranks (group width grows with the period)
+  std::vector<int> r_lo(P->n_classes, nper), r_hi(P->n_classes, 0);
+  for (int r = 0; r < nper; r++) {
+    r_lo[rank_cls[r]] = std::min(r_lo[rank_cls[r]], r);
+    r_hi[rank_cls[r]] = std::max(r_hi[rank_cls[r]], r + 1);
+  }
   std::vector<HostItem> items;
   int64_t tiles_used = 0;
   for (int64_t tile = 0; tile < (int64_t)P->ntx * P->nty; tile++) {
@@ -391,14 +412,14 @@ static int build_plan(gb_plan* P, const gb_geometry* geo, int64_t n_vis, const d
     tiles_used++;
     const int16_t tx = (int16_t)(tile % P->ntx), ty = (int16_t)(tile / P->ntx);
     for (int c = 0; c < P->n_classes; c++) {
-      const double cmax = std::max(4.0 * fixed_cost(c), tau);
+      if (r_lo[c] >= r_hi[c] || offs[k0 + r_hi[c]] == offs[k0 + r_lo[c]]) continue;
+      const double fixed = fixed_cost(c), cmax = std::max(4.0 * fixed, tau);
       HostItem cur{};
       bool open = false;
-      for (int r = 0; r < nper; r++) {
-        if (rank_cls[r] != c) continue;
+      for (int r = r_lo[c]; r < r_hi[c]; r++) {
         int32_t pos = offs[k0 + r];
         const int32_t end = offs[k0 + r + 1];
-        const double rcst = rec_cost(r);
+        const double rcst = rec_cost[r];
         while (pos < end) {
           if (!open) {
             cur.it.start = pos;
@@ -407,7 +428,7 @@ static int build_plan(gb_plan* P, const gb_geometry* geo, int64_t n_vis, const d
             cur.it.tile_y = ty;
             cur.it.pmax = 0;
             cur.it.cls = (int16_t)c;
-            cur.cost = fixed_cost(c);
+            cur.cost = fixed;
             open = true;
           }
           int64_t room = (int64_t)((cmax - cur.cost) / rcst);
@@ -433,20 +454,8 @@ static int build_plan(gb_plan* P, const gb_geometry* geo, int64_t n_vis, const d
   make_bundles(items, P->cls, P->n_classes, it_sorted, bvec);
   P->n_items = (int)it_sorted.size();
   P->n_bundles = (int)bvec.size();
-  // host copy of the items in device order, for batched launches
-  P->host_items.clear();
-  {
-    std::vector<HostItem> by_key = items;
-    // it_sorted is a permutation of items: recover each item's cost by its record range
-    std::sort(by_key.begin(), by_key.end(),
-              [](const HostItem& a, const HostItem& b) { return a.it.start < b.it.start; });
-    for (const Item& it : it_sorted) {
-      auto f = std::lower_bound(by_key.begin(), by_key.end(), it.start,
-                                [](const HostItem& a, int32_t v) { return a.it.start < v; });
-      HostItem h = *f;
-      P->host_items.push_back(h);
-    }
-  }
+  // the items with their costs (any order), for batched launches
+  P->host_items = std::move(items);
 
   // ---- fill
   if ((rc = dalloc(&P->d_recs, P->n_recs)) || (rc = dalloc(&P->d_items, P->n_items)) ||

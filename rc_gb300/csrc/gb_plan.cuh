@@ -153,7 +153,7 @@ struct gb_plan {
   int64_t taps_paired = 0;  // taps of pieces that degridding can take in pairs
   int stage_pref = -1;      // GB_STAGE_*: forced staging form of degridding, or -1
   bool own_plane = true;
-  std::vector<gb::HostItem> host_items;  // in d_items order (grid slot 0)
+  std::vector<gb::HostItem> host_items;  // every item with its cost (grid slot 0)
   // TMA descriptors of the last degridded grid, one per thread-group class
   // (box = that class's stage); rebuilt when the grid's address or shape changes
   const void* tma_grid = nullptr;
