@@ -319,3 +319,30 @@ def test_single_visibility_each_plane():
     grid = torch.zeros((G, G), dtype=torch.complex64, device="cuda")
     P.grid(torch.tensor(c["vis"], dtype=torch.complex64, device="cuda"), d_gcf, grid)
     assert rel_l2(grid.cpu().numpy(), oracle_grid(c)) < TOL32
+
+
+def test_gcf_on_an_8_byte_boundary():
+    """A GCF array that starts 8 bytes past a 16-byte boundary: no tap pairs
+    (their 16-byte loads need the alignment), so the automatic staging takes
+    plain rows; forced split rows read every tap on its own.  Both against the
+    oracle."""
+    torch = torch_mod()
+    from rc_gb300 import lib
+
+    c = random_case(14, supports=(8, 16, 40))
+    P = make_plan(c, tile=24, threads=256, cap=40)
+    buf = torch.zeros(len(c["gcf"]) + 1, dtype=torch.complex64, device="cuda")
+    buf[1:] = torch.tensor(c["gcf"], dtype=torch.complex64, device="cuda")
+    d_gcf = buf[1:]
+    assert d_gcf.data_ptr() % 16 == 8
+    model = np.random.default_rng(15).standard_normal((c["G"], c["G"])) * (1 + 0.5j)
+    d_model = torch.tensor(model, dtype=torch.complex64, device="cuda")
+    for stage, want in [(lib.STAGE_AUTO, lib.STAGE_TMA), (lib.STAGE_SPLIT, lib.STAGE_SPLIT)]:
+        P.set_stage(stage)
+        for mode in (0, 1):
+            pred = P.degrid(d_gcf, d_model, mode=mode).cpu().numpy()
+            assert rel_l2(pred, oracle_degrid(c, model, mode)) < TOL32, (stage, mode)
+        assert P.device_status() == (0, want)
+    grid = torch.zeros((c["G"], c["G"]), dtype=torch.complex64, device="cuda")
+    P.grid(torch.tensor(c["vis"], dtype=torch.complex64, device="cuda"), d_gcf, grid)
+    assert rel_l2(grid.cpu().numpy(), oracle_grid(c)) < TOL32
