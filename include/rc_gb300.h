@@ -172,6 +172,12 @@ int gb_plan_stats(const gb_plan *plan, int64_t *stats7);
 #define GB_STAGE_ROWS 2
 int gb_plan_set_stage(gb_plan *plan, int32_t stage);
 
+/* Test hook (host-side fault injection): let the next `after` device
+ * allocations of the library succeed and fail the `count` after them with
+ * GB_ERR_NOMEM, as a cudaMalloc out of memory would.  (0, 0) turns it off.
+ * Every entry point then returns its error and leaves no partial object. */
+int gb_debug_fail_allocs(int32_t after, int32_t count);
+
 /* Device-side status of a plan's degridding, read synchronously on `stream`:
  * out2[0] = 1 when a TMA stage of a degridding launch did not complete within
  * its bounded wait since the last call (that launch's predictions are then

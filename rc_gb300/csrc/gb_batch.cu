@@ -130,10 +130,13 @@ static int batch_build(gb_batch* B, int32_t n, const gb_batch_member* m, cudaStr
   make_bundles(items, B->cls, B->n_classes, it_out, b_out);
   B->n_items = (int)it_out.size();
   B->n_bundles = (int)b_out.size();
-  GB_CUDA_TRY(cudaMalloc(&B->d_recs, sizeof(Rec) * (B->n_recs ? B->n_recs : 1)));
-  GB_CUDA_TRY(cudaMalloc(&B->d_items, sizeof(Item) * (B->n_items ? B->n_items : 1)));
-  GB_CUDA_TRY(cudaMalloc(&B->d_bundles, sizeof(Bundle) * (B->n_bundles ? B->n_bundles : 1)));
-  GB_CUDA_TRY(cudaMalloc(&B->d_queue, sizeof(int32_t) * 2));
+  if ((rc = dev_alloc((void**)&B->d_recs, sizeof(Rec) * (B->n_recs ? B->n_recs : 1), "batch")) ||
+      (rc = dev_alloc((void**)&B->d_items, sizeof(Item) * (B->n_items ? B->n_items : 1),
+                      "batch")) ||
+      (rc = dev_alloc((void**)&B->d_bundles,
+                      sizeof(Bundle) * (B->n_bundles ? B->n_bundles : 1), "batch")) ||
+      (rc = dev_alloc((void**)&B->d_queue, sizeof(int32_t) * 2, "batch")))
+    return rc;
   off = 0;
   for (gb_plan* p : B->members) {
     if (p->n_recs)

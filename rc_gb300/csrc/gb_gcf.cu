@@ -168,9 +168,10 @@ extern "C" int gb_gcf_generate(int32_t n_planes, const double* w_planes, const i
   cufftHandle plan = 0;
   bool have_plan = false;
   int nfft[2] = {N, N};
-  GB_CUDA_GOTO(cudaMalloc(&d_planes, sizeof(GcfPlaneDev) * n_planes));
-  GB_CUDA_GOTO(cudaMalloc(&arena, arena_bytes * batch));
-  GB_CUDA_GOTO(cudaMalloc(&sums, sizeof(double) * GB_PHASES * batch));
+  if ((rc = dev_alloc((void**)&d_planes, sizeof(GcfPlaneDev) * n_planes, "GCF generation")) ||
+      (rc = dev_alloc((void**)&arena, arena_bytes * batch, "GCF generation")) ||
+      (rc = dev_alloc((void**)&sums, sizeof(double) * GB_PHASES * batch, "GCF generation")))
+    goto done;
   GB_CUDA_GOTO(cudaMemcpyAsync(d_planes, hp.data(), sizeof(GcfPlaneDev) * n_planes,
                                cudaMemcpyHostToDevice, s));
   GB_CUFFT_TRY(cufftPlanMany(&plan, 2, nfft, nullptr, 1, N * N, nullptr, 1, N * N, CUFFT_Z2Z, batch));

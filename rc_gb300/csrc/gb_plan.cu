@@ -172,13 +172,10 @@ static void free_plan(gb_plan* p) {
 
 template <class T>
 static int dalloc(T** p, size_t n) {
-  cudaError_t e = cudaMalloc((void**)p, sizeof(T) * (n ? n : 1));
-  if (e != cudaSuccess) {
-    *p = nullptr;
-    gb_set_error(GB_ERR_NOMEM, "cudaMalloc(%zu): %s", sizeof(T) * n, cudaGetErrorString(e));
-    return GB_ERR_NOMEM;
-  }
-  return GB_OK;
+  void* q = nullptr;
+  const int rc = dev_alloc(&q, sizeof(T) * (n ? n : 1), "plan");
+  *p = (T*)q;
+  return rc;
 }
 
 void make_bundles(const std::vector<HostItem>& items, const ClassInfo* cls, int n_classes,

@@ -69,6 +69,35 @@ int stage_stream(cudaStream_t* out) {
   return GB_OK;
 }
 
+// ---------------------------------------------------------------- allocations
+// Host-side fault injection for tests: let `g_fail_after` more allocations
+// succeed, then fail the next `g_fail_count` (no GPU fault involved).
+static std::mutex g_fail_mu;
+static int g_fail_after = 0, g_fail_count = 0;
+
+int dev_alloc(void** p, size_t bytes, const char* what) {
+  *p = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(g_fail_mu);
+    if (g_fail_count > 0) {
+      if (g_fail_after > 0) {
+        g_fail_after--;
+      } else {
+        g_fail_count--;
+        gb_set_error(GB_ERR_NOMEM, "%s: allocation of %zu bytes failed (injected)", what, bytes);
+        return GB_ERR_NOMEM;
+      }
+    }
+  }
+  const cudaError_t e = cudaMalloc(p, bytes ? bytes : 16);
+  if (e != cudaSuccess) {
+    *p = nullptr;
+    gb_set_error(GB_ERR_NOMEM, "%s: cudaMalloc(%zu): %s", what, bytes, cudaGetErrorString(e));
+    return GB_ERR_NOMEM;
+  }
+  return GB_OK;
+}
+
 int stage_buffer(int slot, size_t bytes, void** out) {
   if (slot < 0 || slot >= kStageSlots) {
     gb_set_error(GB_ERR_ARG, "staging slot %d out of range", slot);
@@ -80,11 +109,8 @@ int stage_buffer(int slot, size_t bytes, void** out) {
     t_stage.buf[slot] = nullptr;
     t_stage.cap[slot] = 0;
     size_t grow = bytes + bytes / 4;
-    cudaError_t e = cudaMalloc(&t_stage.buf[slot], grow);
-    if (e != cudaSuccess) {
-      gb_set_error(GB_ERR_NOMEM, "cudaMalloc(%zu) for staging: %s", grow, cudaGetErrorString(e));
-      return GB_ERR_NOMEM;
-    }
+    const int rc = dev_alloc(&t_stage.buf[slot], grow, "staging buffer");
+    if (rc) return rc;
     t_stage.cap[slot] = grow;
   }
   *out = t_stage.buf[slot];
@@ -119,5 +145,16 @@ extern "C" int gb_grid_zero_f32(float* d_grid, int64_t n_complex, void* stream) 
   }
   if (n_complex == 0) return GB_OK;
   GB_CUDA_TRY(cudaMemsetAsync(d_grid, 0, (size_t)n_complex * 8, (cudaStream_t)stream));
+  return GB_OK;
+}
+
+extern "C" int gb_debug_fail_allocs(int32_t after, int32_t count) {
+  if (after < 0 || count < 0) {
+    gb_set_error(GB_ERR_ARG, "gb_debug_fail_allocs: negative argument");
+    return GB_ERR_ARG;
+  }
+  std::lock_guard<std::mutex> lk(gb::g_fail_mu);
+  gb::g_fail_after = after;
+  gb::g_fail_count = count;
   return GB_OK;
 }

@@ -15,6 +15,10 @@ int stage_buffer(int slot, size_t bytes, void** out);
 
 int sm_count();
 
+// Every device allocation of the library goes through here: cudaMalloc, or
+// GB_ERR_NOMEM when the allocation-failure hook (gb_debug_fail_allocs) says so.
+int dev_alloc(void** p, size_t bytes, const char* what);
+
 __global__ void k_zero_f32x2(float2* __restrict__ p, int64_t n);
 
 }  // namespace gb

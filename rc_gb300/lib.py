@@ -132,6 +132,7 @@ SIGNATURES = {
     "gb_plan_stats": (C.c_int, [_VP, C.POINTER(C.c_int64)]),
     "gb_plan_device_status": (C.c_int, [_VP, C.POINTER(C.c_int32), _VP]),
     "gb_plan_set_stage": (C.c_int, [_VP, C.c_int32]),
+    "gb_debug_fail_allocs": (C.c_int, [C.c_int32, C.c_int32]),
     "kern_fft": (C.c_int, [_VP, _VP]),
     "kern_ifft": (C.c_int, [_VP, _VP]),
     "gb_plan_export_index": (C.c_int, [_VP, _VP, _VP]),
