@@ -178,6 +178,16 @@ int gb_plan_set_stage(gb_plan *plan, int32_t stage);
  * Every entry point then returns its error and leaves no partial object. */
 int gb_debug_fail_allocs(int32_t after, int32_t count);
 
+/* Bounds-checked build (compiled with -DGB_CHECKED: rc_gb300.build(checked=True),
+ * librc_gb300_checked.so): the FP32 tiled kernels test every shared-memory,
+ * GCF, record and visibility index against its array, count violations in a
+ * device word and redirect the access to element 0.  gb_checked_violations
+ * returns the count since its last call and clears it (-1 in the normal
+ * build); gb_checked_selftest counts two out-of-range indices without touching
+ * memory (GB_ERR_ARG in the normal build). */
+int gb_checked_violations(int64_t *out);
+int gb_checked_selftest(void);
+
 /* Device-side status of a plan's degridding, read synchronously on `stream`:
  * out2[0] = 1 when a TMA stage of a degridding launch did not complete within
  * its bounded wait since the last call (that launch's predictions are then

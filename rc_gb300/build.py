@@ -20,6 +20,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "librc_gb300.so")
+# the bounds-checked variant (-DGB_CHECKED), built on request
+LIB_CHECKED = os.path.join(HERE, "librc_gb300_checked.so")
+BUILD_CHECKED = os.path.join(HERE, "_build_checked")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -44,25 +47,31 @@ def _deps():
         os.path.abspath(__file__)]
 
 
-def up_to_date() -> bool:
-    if not os.path.exists(LIB):
+def up_to_date(lib: str = LIB) -> bool:
+    if not os.path.exists(lib):
         return False
-    t = os.path.getmtime(LIB)
+    t = os.path.getmtime(lib)
     return all(os.path.getmtime(d) <= t for d in _deps())
 
 
-def build(force: bool = False, ptxas_verbose: bool = False, verbose: bool = False) -> str:
-    if not force and up_to_date():
-        return LIB
-    os.makedirs(BUILD, exist_ok=True)
+def build(force: bool = False, ptxas_verbose: bool = False, verbose: bool = False,
+          checked: bool = False) -> str:
+    """Build the library; checked=True builds the bounds-checked variant
+    (librc_gb300_checked.so, -DGB_CHECKED) instead."""
+    lib_out, build_dir = (LIB_CHECKED, BUILD_CHECKED) if checked else (LIB, BUILD)
+    if not force and up_to_date(lib_out):
+        return lib_out
+    os.makedirs(build_dir, exist_ok=True)
     cc = nvcc()
     flags = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", INCLUDE,
                     "--expt-relaxed-constexpr"]
+    if checked:
+        flags += ["-DGB_CHECKED"]
     if ptxas_verbose:
         flags += ["-Xptxas", "-v"]
 
     def one(src):
-        obj = os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")
+        obj = os.path.join(build_dir, os.path.basename(src)[:-3] + ".o")
         cmd = [cc] + flags + ["-c", src, "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
@@ -77,14 +86,14 @@ def build(force: bool = False, ptxas_verbose: bool = False, verbose: bool = Fals
                 print(f"--- {os.path.basename(obj)}\n{err}", file=sys.stderr)
     objs = [o for o, _ in results]
     libdir = os.path.join(cuda_home(), "lib64")
-    tmp = LIB + ".tmp"
+    tmp = lib_out + ".tmp"
     cmd = [cc] + ARCH + ["-shared", "-o", tmp] + objs + [
         "-L", libdir, "-lcufft", "-Xlinker", "-rpath," + libdir]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, lib_out)
+    return lib_out
 
 
 def main(argv=None):

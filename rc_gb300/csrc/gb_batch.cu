@@ -34,6 +34,7 @@ struct gb_batch {
   int64_t n_recs = 0;
   int n_items = 0, n_bundles = 0;
   int64_t kept = 0, taps = 0, taps_paired = 0;
+  int64_t gcf_len = 0;
 };
 
 using namespace gb;
@@ -119,6 +120,7 @@ static int batch_build(gb_batch* B, int32_t n, const gb_batch_member* m, cudaStr
     B->kept += p->kept;
     B->taps += p->taps;
     B->taps_paired += p->taps_paired;
+    B->gcf_len = std::max(B->gcf_len, p->gcf_len);
   }
   B->n_recs = off;
   if (B->n_recs >= (int64_t)INT32_MAX) {
@@ -211,6 +213,9 @@ static int fill_slots(const gb_batch* B, float* const* grids, float* const* vis,
     gp->s[i].pitch = p->dev.pitch;
     gp->s[i].ext_x = p->dev.ext_x;
     gp->s[i].ext_y = p->dev.ext_y;
+#ifdef GB_CHECKED
+    gp->s[i].n_vis = p->dev.n_vis;
+#endif
   }
   return GB_OK;
 }
@@ -226,7 +231,8 @@ extern "C" int gb_batch_grid_f32(gb_batch* B, const float* const* d_vis, const f
   if (rc) return rc;
   return launch_tiled_batch(true, 0, B->NT, B->smem_grid, B->ctas_grid, B->d_bundles,
                             B->n_bundles, B->d_items, B->d_recs, B->d_queue, B->cls,
-                            B->n_classes, B->T, gp, d_gcf, 0, (cudaStream_t)stream);
+                            B->n_classes, B->T, gp, d_gcf, 0,
+                            TiledBounds{B->n_recs, B->gcf_len, 0}, (cudaStream_t)stream);
 }
 
 extern "C" int gb_batch_degrid_f32(gb_batch* B, const float* d_gcf, const float* const* d_grids,
@@ -246,7 +252,8 @@ extern "C" int gb_batch_degrid_f32(gb_batch* B, const float* d_gcf, const float*
   const int stage = degrid_stage_choice(-1, B->taps, B->taps_paired, d_gcf, false);
   return launch_tiled_batch(false, mode, B->NT, B->smem_degrid, B->ctas_degrid[stage], B->d_bundles,
                             B->n_bundles, B->d_items, B->d_recs, B->d_queue, B->cls,
-                            B->n_classes, B->T, gp, d_gcf, stage, s);
+                            B->n_classes, B->T, gp, d_gcf, stage,
+                            TiledBounds{B->n_recs, B->gcf_len, 0}, s);
 }
 
 // Plain FP64 path over the members (one launch each): the comparison path of

@@ -271,6 +271,7 @@ extern "C" int gb_grid_f32_noalloc(const gb_geometry* geo, int64_t n_vis, const 
   // planes -> pieces, periods, classes (the rules of gb_plan_create)
   thread_local PlaneInfo pl[kMaxPlanes];
   int widths[kMaxClasses], nwidth = 0, kmax = 1;
+  int64_t gcf_len = 0;
   for (int p = 0; p < geo->n_planes; p++) {
     const int S = geo->supports[p];
     if (S < 1 || S > GB_MAX_SUPPORT || geo->gcf_offsets[p] < 0 ||
@@ -284,6 +285,7 @@ extern "C" int gb_grid_f32_noalloc(const gb_geometry* geo, int64_t n_vis, const 
     q.k = (S + cap - 1) / cap;
     q.P = (S + q.k - 1) / q.k;
     q.gcf_off = geo->gcf_offsets[p];
+    gcf_len = std::max<int64_t>(gcf_len, q.gcf_off + (int64_t)GB_PHASES * S * S);
     kmax = q.k > kmax ? q.k : kmax;
     const int L = class_width_na(q.P, NT);
     int c = 0;
@@ -400,5 +402,5 @@ extern "C" int gb_grid_f32_noalloc(const gb_geometry* geo, int64_t n_vis, const 
   }
   return launch_grid_tiled_tables(bundles, hc[kCntBundles], items, recs, counters + kCntQueue, cls,
                                   nwidth, NT, T, geo->ext_x, geo->ext_y, geo->pitch, smem, d_vis,
-                                  d_gcf, d_grid, s);
+                                  d_gcf, d_grid, TiledBounds{hc[kCntPieces], gcf_len, n_vis}, s);
 }

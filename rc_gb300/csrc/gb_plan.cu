@@ -243,6 +243,7 @@ static int build_plan(gb_plan* P, const gb_geometry* geo, int64_t n_vis, const d
     q.k = (q.S + P->pcap - 1) / P->pcap;
     q.P = (q.S + q.k - 1) / q.k;
     q.gcf_off = geo->gcf_offsets[p];
+    P->gcf_len = std::max<int64_t>(P->gcf_len, q.gcf_off + (int64_t)GB_PHASES * q.S * q.S);
     periods.push_back(q.P);
     if (q.gcf_off + (int64_t)GB_PHASES * q.S * q.S > (int64_t)UINT32_MAX) {
       gb_set_error(GB_ERR_CAPACITY, "GCF array exceeds 2^32 complex elements");

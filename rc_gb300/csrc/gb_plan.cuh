@@ -108,6 +108,9 @@ struct GridSlot {
   float2* vis;
   int64_t pitch;
   int32_t ext_x, ext_y;
+#ifdef GB_CHECKED
+  int64_t n_vis;  // visibilities behind `vis` (the bounds-checked build tests indices)
+#endif
 };
 struct GridPtrs {
   GridSlot s[kMaxGrids];
@@ -151,6 +154,7 @@ struct gb_plan {
   int n_items = 0, n_bundles = 0;
   int64_t kept = 0, taps = 0, tiles_used = 0;
   int64_t taps_paired = 0;  // taps of pieces that degridding can take in pairs
+  int64_t gcf_len = 0;      // complex elements the planes' GCFs span
   int stage_pref = -1;      // GB_STAGE_*: forced staging form of degridding, or -1
   bool own_plane = true;
   std::vector<gb::HostItem> host_items;  // every item with its cost (grid slot 0)
@@ -182,14 +186,20 @@ int launch_degrid_tiled(gb_plan* plan, const float* gcf, const float* grid, floa
 size_t tiled_smem_grid(const ClassInfo* cls, int n_classes, int NT);
 size_t tiled_smem_degrid(const ClassInfo* cls, int n_classes, int NT);
 int tiled_max_smem();
+// Array sizes behind a launch's pointers (used by the bounds-checked build).
+struct TiledBounds {
+  int64_t n_recs, gcf_len, n_vis;
+};
 int launch_grid_tiled_tables(const Bundle* bundles, int n_bundles, const Item* items,
                              const Rec* recs, int32_t* queue, const ClassInfo* cls, int n_classes,
                              int NT, int T, int ext_x, int ext_y, int64_t pitch, size_t smem,
-                             const float* vis, const float* gcf, float* grid, cudaStream_t s);
+                             const float* vis, const float* gcf, float* grid,
+                             const TiledBounds& bounds, cudaStream_t s);
 int launch_tiled_batch(bool grid_mode, int mode, int NT, size_t smem, int ctas_per_sm,
                        const Bundle* bundles, int n_bundles, const Item* items, const Rec* recs,
                        int32_t* queue, const ClassInfo* cls, int n_classes, int T,
-                       const GridPtrs& gp, const float* gcf, int stage, cudaStream_t s);
+                       const GridPtrs& gp, const float* gcf, int stage,
+                       const TiledBounds& bounds, cudaStream_t s);
 // Staging form of a degridding launch (GB_STAGE_SPLIT / _TMA / _ROWS): split
 // rows when at least half of the taps are paired and the GCF allows pairs.
 int degrid_stage_choice(int pref, int64_t taps, int64_t taps_paired, const float* gcf,

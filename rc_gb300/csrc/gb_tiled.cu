@@ -44,7 +44,30 @@ struct TiledArgs {
   ClassInfo cls[kMaxClasses];
   int32_t n_bundles;
   int32_t T;
+#ifdef GB_CHECKED
+  int64_t n_recs;   // records in `recs`
+  int64_t gcf_len;  // complex elements in the GCF array
+#endif
 };
+
+// Checked build (-DGB_CHECKED, rc_gb300.build(checked=True)): every shared
+// memory, GCF, record and visibility index below is tested against its
+// array; a violation is counted in g_check_violations (gb_checked_violations)
+// and the access goes to element 0 instead.  No trap, no fault: the counter is
+// how tests see it.  In the normal build GB_IDX is the index itself.
+#ifdef GB_CHECKED
+__device__ unsigned long long g_check_violations;
+__device__ __forceinline__ int64_t gb_checked_index(int64_t i, int64_t lim) {
+  if (i < 0 || i >= lim) {
+    atomicAdd(&g_check_violations, 1ull);
+    return 0;
+  }
+  return i;
+}
+#define GB_IDX(i, lim) gb_checked_index((int64_t)(i), (int64_t)(lim))
+#else
+#define GB_IDX(i, lim) (i)
+#endif
 
 __device__ __forceinline__ void group_sync(int id, int n, bool whole_cta) {
   if (whole_cta)
@@ -112,7 +135,8 @@ template <int R, int U, bool FULL>
 __device__ __forceinline__ void grid_run(int k, int e, int lt, int L, int As,
                                          const GridRec* __restrict__ srec,
                                          float4* __restrict__ acc,
-                                         const float2* __restrict__ gcf) {
+                                         const float2* __restrict__ gcf, int acc_len,
+                                         int64_t gcf_len) {
   const int P = shape_period(srec[k].shape);
   int ra[R], rb[R];
   bool own[R];  // slot m holds a residue (R L may exceed P^2)
@@ -144,7 +168,8 @@ __device__ __forceinline__ void grid_run(int k, int e, int lt, int L, int As,
           i += i < 0 ? P : 0;
           int j = rb[m] - r.ym;
           j += j < 0 ? P : 0;
-          c[u][m] = own[m] ? __ldg(gcf + r.gcf + j * r.pitch + i) : make_float2(0.f, 0.f);
+          c[u][m] = own[m] ? __ldg(gcf + GB_IDX(r.gcf + j * r.pitch + i, gcf_len))
+                           : make_float2(0.f, 0.f);
           qi[u][m] = r.q0 + j * As + i;
         }
       }
@@ -153,7 +178,7 @@ __device__ __forceinline__ void grid_run(int k, int e, int lt, int L, int As,
 #pragma unroll
         for (int m = 0; m < R; m++) {
           if (own[m]) {
-            const int q = qi[u][m];
+            const int q = GB_IDX(qi[u][m], acc_len);
             const float tr = v[u].x * c[u][m].x - v[u].y * c[u][m].y;
             const float ti = v[u].x * c[u][m].y + v[u].y * c[u][m].x;
             float4 s = acc[q];
@@ -181,7 +206,7 @@ __device__ __forceinline__ void grid_run(int k, int e, int lt, int L, int As,
         int j = rb[m] - r.ym;
         j += j < 0 ? P : 0;
         if (live && own[m] && (FULL || (i < shape_wx(r.shape) && j < shape_wy(r.shape)))) {
-          c[u][m] = __ldg(gcf + r.gcf + j * r.pitch + i);
+          c[u][m] = __ldg(gcf + GB_IDX(r.gcf + j * r.pitch + i, gcf_len));
           qi[u][m] = r.q0 + j * As + i;
         } else {
           c[u][m] = make_float2(0.f, 0.f);
@@ -193,8 +218,8 @@ __device__ __forceinline__ void grid_run(int k, int e, int lt, int L, int As,
     for (int u = 0; u < U; u++) {
 #pragma unroll
       for (int m = 0; m < R; m++) {
-        const int q = qi[u][m];
-        if (q >= 0) {
+        if (qi[u][m] >= 0) {
+          const int q = GB_IDX(qi[u][m], acc_len);
           const float tr = v[u].x * c[u][m].x - v[u].y * c[u][m].y;
           const float ti = v[u].x * c[u][m].y + v[u].y * c[u][m].x;
           float4 s = acc[q];
@@ -211,15 +236,16 @@ template <bool FULL>
 __device__ __forceinline__ void grid_dispatch(int slots, int k, int e, int lt, int L, int As,
                                               const GridRec* __restrict__ srec,
                                               float4* __restrict__ acc,
-                                              const float2* __restrict__ gcf) {
+                                              const float2* __restrict__ gcf, int acc_len,
+                                              int64_t gcf_len) {
   switch (slots) {
-    case 1: grid_run<1, 8, FULL>(k, e, lt, L, As, srec, acc, gcf); break;
-    case 2: grid_run<2, 4, FULL>(k, e, lt, L, As, srec, acc, gcf); break;
-    case 3: grid_run<3, 3, FULL>(k, e, lt, L, As, srec, acc, gcf); break;
-    case 4: grid_run<4, 2, FULL>(k, e, lt, L, As, srec, acc, gcf); break;
+    case 1: grid_run<1, 8, FULL>(k, e, lt, L, As, srec, acc, gcf, acc_len, gcf_len); break;
+    case 2: grid_run<2, 4, FULL>(k, e, lt, L, As, srec, acc, gcf, acc_len, gcf_len); break;
+    case 3: grid_run<3, 3, FULL>(k, e, lt, L, As, srec, acc, gcf, acc_len, gcf_len); break;
+    case 4: grid_run<4, 2, FULL>(k, e, lt, L, As, srec, acc, gcf, acc_len, gcf_len); break;
     case 5:
-    case 6: grid_run<6, 1, FULL>(k, e, lt, L, As, srec, acc, gcf); break;
-    default: grid_run<8, 1, FULL>(k, e, lt, L, As, srec, acc, gcf); break;
+    case 6: grid_run<6, 1, FULL>(k, e, lt, L, As, srec, acc, gcf, acc_len, gcf_len); break;
+    default: grid_run<8, 1, FULL>(k, e, lt, L, As, srec, acc, gcf, acc_len, gcf_len); break;
   }
 }
 
@@ -232,6 +258,11 @@ __device__ __forceinline__ void grid_item(const TiledArgs& a, const Item& it, in
   const float2* __restrict__ vis = gs.vis;
   float2* __restrict__ grid = gs.grid;
   const int As = acc_stride(A), AA = A * As;
+#ifdef GB_CHECKED
+  const int64_t gcf_len = a.gcf_len;
+#else
+  const int64_t gcf_len = 0;
+#endif
   for (int q = lt; q < AA; q += L) acc[q] = make_float4(0.f, 0.f, 0.f, 0.f);
   int curP = -1;
   const int end = it.start + it.count;
@@ -239,7 +270,7 @@ __device__ __forceinline__ void grid_item(const TiledArgs& a, const Item& it, in
     const int nb = min(L, end - base);
     group_sync(bar, L, whole);  // zeroing done / previous batch consumed
     if (lt < nb) {
-      const Rec r = a.recs[base + lt];
+      const Rec r = a.recs[GB_IDX(base + lt, a.n_recs)];
       GridRec d;
       d.gcf = (int32_t)r.gcf;
       d.q0 = r.yl * As + r.xl;
@@ -248,7 +279,7 @@ __device__ __forceinline__ void grid_item(const TiledArgs& a, const Item& it, in
       d.pitch = r.sm1 + 1;
       d.shape = (r.pm1 + 1) | (r.wx << 9) | (r.wy << 18) |
                 (r.wx == r.pm1 + 1 && r.wy == r.pm1 + 1 ? kWholePiece : 0);
-      d.vis = __ldg(vis + r.vis);
+      d.vis = __ldg(vis + GB_IDX(r.vis, gs.n_vis));
       srec[lt] = d;
     }
     group_sync(bar, L, whole);
@@ -281,8 +312,10 @@ __device__ __forceinline__ void grid_item(const TiledArgs& a, const Item& it, in
         full = full && mp == 0;
         e += 32;
       }
-      if (full) grid_dispatch<true>(slots_for(P, L), k, e, lt, L, As, srec, acc, gcf);
-      else grid_dispatch<false>(slots_for(P, L), k, e, lt, L, As, srec, acc, gcf);
+      if (full)
+        grid_dispatch<true>(slots_for(P, L), k, e, lt, L, As, srec, acc, gcf, AA, gcf_len);
+      else
+        grid_dispatch<false>(slots_for(P, L), k, e, lt, L, As, srec, acc, gcf, AA, gcf_len);
       k = e;
     }
   }
@@ -445,6 +478,16 @@ __device__ __forceinline__ void degrid_item(const TiledArgs& a, const Item& it, 
   // lanes, whatever the parity of the piece's first column.
   const int He = Ae >> 1;
   const int x0 = it.tile_x * a.T, y0 = it.tile_y * a.T;
+  // array sizes for the bounds-checked build (unused otherwise)
+  const int stage_len = A * Ae;
+#ifdef GB_CHECKED
+  const int64_t gcf_len = a.gcf_len;
+#else
+  const int64_t gcf_len = 0;
+#endif
+  const int64_t gcf_pairs = gcf_len / 2;
+  (void)stage_len;
+  (void)gcf_pairs;
   if constexpr (TMA) {
     if (lt == 0) {
       // the stage's earlier reads (generic proxy) come before the copy's writes
@@ -469,7 +512,7 @@ __device__ __forceinline__ void degrid_item(const TiledArgs& a, const Item& it, 
         py++;
       }
       const float2* src = in ? grid + (int64_t)gy * gs.pitch + gx : grid;
-      const unsigned dst = (unsigned)__cvta_generic_to_shared(sg + sq);
+      const unsigned dst = (unsigned)__cvta_generic_to_shared(sg + GB_IDX(sq, AA));
       asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(dst), "l"(src),
                    "r"(in ? 8 : 0)
                    : "memory");
@@ -485,7 +528,7 @@ __device__ __forceinline__ void degrid_item(const TiledArgs& a, const Item& it, 
     const int nb = min(L, end - base);
     group_sync(bar, L, whole);  // previous batch consumed
     if (lt < nb) {
-      const Rec r = a.recs[base + lt];
+      const Rec r = a.recs[GB_IDX(base + lt, a.n_recs)];
       DegridRec d;
       d.gcf = (int32_t)r.gcf;
       d.pitch = r.sm1 + 1;
@@ -570,9 +613,10 @@ __device__ __forceinline__ void degrid_item(const TiledArgs& a, const Item& it, 
 #pragma unroll
             for (int u = 0; u < UN; u++) {
               const bool ok = !CHECK || t + u < n;
-              c[u] = ok ? __ldg(gp + off_g[u]) : make_float4(0.f, 0.f, 0.f, 0.f);
-              x0[u] = ok ? sp[off_s[u]] : make_float2(0.f, 0.f);
-              x1[u] = ok ? sp1[off_s[u]] : make_float2(0.f, 0.f);
+              c[u] = ok ? __ldg(gp + GB_IDX(off_g[u], gcf_pairs - r.gcf / 2))
+                        : make_float4(0.f, 0.f, 0.f, 0.f);
+              x0[u] = ok ? sp[GB_IDX(off_s[u], stage_len - r.q0)] : make_float2(0.f, 0.f);
+              x1[u] = ok ? sp1[GB_IDX(off_s[u], stage_len - (sp1 - sg))] : make_float2(0.f, 0.f);
             }
             // the group's products summed by FMA chains, then one compensated
             // add of the group sum
@@ -619,8 +663,8 @@ __device__ __forceinline__ void degrid_item(const TiledArgs& a, const Item& it, 
 #pragma unroll
             for (int u = 0; u < UN; u++) {
               const bool ok = !CHECK || t + u < n;
-              c[u] = ok ? __ldg(gp + off_g[u]) : make_float2(0.f, 0.f);
-              x[u] = ok ? sp[off_s[u]] : make_float2(0.f, 0.f);
+              c[u] = ok ? __ldg(gp + GB_IDX(off_g[u], gcf_len - r.gcf)) : make_float2(0.f, 0.f);
+              x[u] = ok ? sp[GB_IDX(off_s[u], stage_len - r.q0)] : make_float2(0.f, 0.f);
             }
             float br = 0.f, bi = 0.f;
 #pragma unroll
@@ -646,9 +690,9 @@ __device__ __forceinline__ void degrid_item(const TiledArgs& a, const Item& it, 
       }
       if (live && sl == 0) {
         if (r.flags & kRecCut)
-          atomicAdd(pred + r.vis, make_float2(ar, ai));
+          atomicAdd(pred + GB_IDX(r.vis, gs.n_vis), make_float2(ar, ai));
         else
-          pred[r.vis] = make_float2(ar, ai);
+          pred[GB_IDX(r.vis, gs.n_vis)] = make_float2(ar, ai);
       }
     }
   }
@@ -773,6 +817,16 @@ int tiled_ctas_per_sm(const gb_plan* P, bool grid, int stage) {
   return n > 0 ? n : 1;
 }
 
+static void set_bounds(TiledArgs& a, const TiledBounds& b) {
+#ifdef GB_CHECKED
+  a.n_recs = b.n_recs;
+  a.gcf_len = b.gcf_len;
+#else
+  (void)a;
+  (void)b;
+#endif
+}
+
 static TiledArgs make_args(const gb_plan* P) {
   TiledArgs a;
   a.bundles = P->d_bundles;
@@ -782,11 +836,12 @@ static TiledArgs make_args(const gb_plan* P) {
   for (int c = 0; c < kMaxClasses; c++) a.cls[c] = P->cls[c];
   a.n_bundles = P->n_bundles;
   a.T = P->T;
+  set_bounds(a, TiledBounds{P->n_recs, P->gcf_len, P->dev.n_vis});
   return a;
 }
 
 static GridPtrs one_grid(const float* grid, const float* vis, int ext_x, int ext_y,
-                         int64_t pitch) {
+                         int64_t pitch, int64_t n_vis) {
   GridPtrs gp;
   memset(&gp, 0, sizeof(gp));
   gp.s[0].grid = (float2*)grid;
@@ -794,6 +849,11 @@ static GridPtrs one_grid(const float* grid, const float* vis, int ext_x, int ext
   gp.s[0].pitch = pitch;
   gp.s[0].ext_x = ext_x;
   gp.s[0].ext_y = ext_y;
+#ifdef GB_CHECKED
+  gp.s[0].n_vis = n_vis;
+#else
+  (void)n_vis;
+#endif
   return gp;
 }
 
@@ -804,7 +864,7 @@ int launch_grid_tiled(gb_plan* P, const float* vis, const float* gcf, float* gri
   const int blocks = std::min(P->n_bundles, sm_count() * P->ctas_per_sm_grid);
   GridFn fn = grid_fn(P->NT);
   fn<<<blocks, P->NT, P->smem_grid, s>>>(
-      make_args(P), one_grid(grid, vis, P->dev.ext_x, P->dev.ext_y, P->dev.pitch),
+      make_args(P), one_grid(grid, vis, P->dev.ext_x, P->dev.ext_y, P->dev.pitch, P->dev.n_vis),
       (const float2*)gcf);
   GB_CUDA_TRY(cudaGetLastError());
   return GB_OK;
@@ -889,8 +949,8 @@ int launch_degrid_tiled(gb_plan* P, const float* gcf, const float* grid, float* 
   const int blocks = std::min(P->n_bundles, sm_count() * P->ctas_per_sm_degrid[stage]);
   DegridFn fn = degrid_fn(P->NT, mode, stage);
   fn<<<blocks, P->NT, P->smem_degrid, s>>>(
-      make_args(P), one_grid(grid, pred, P->dev.ext_x, P->dev.ext_y, P->dev.pitch), sm,
-      (const float2*)gcf);
+      make_args(P), one_grid(grid, pred, P->dev.ext_x, P->dev.ext_y, P->dev.pitch, P->dev.n_vis),
+      sm, (const float2*)gcf);
   GB_CUDA_TRY(cudaGetLastError());
   return GB_OK;
 }
@@ -901,7 +961,8 @@ int launch_degrid_tiled(gb_plan* P, const float* gcf, const float* grid, float* 
 int launch_grid_tiled_tables(const Bundle* bundles, int n_bundles, const Item* items,
                              const Rec* recs, int32_t* queue, const ClassInfo* cls, int n_classes,
                              int NT, int T, int ext_x, int ext_y, int64_t pitch, size_t smem,
-                             const float* vis, const float* gcf, float* grid, cudaStream_t s) {
+                             const float* vis, const float* gcf, float* grid,
+                             const TiledBounds& bounds, cudaStream_t s) {
   if (n_bundles <= 0) return GB_OK;
   GridFn fn = grid_fn(NT);
   int rc = set_smem_attr((const void*)fn);
@@ -917,8 +978,10 @@ int launch_grid_tiled_tables(const Bundle* bundles, int n_bundles, const Item* i
   for (int c = 0; c < kMaxClasses; c++) a.cls[c] = c < n_classes ? cls[c] : ClassInfo{64, 1, 1, 1};
   a.n_bundles = n_bundles;
   a.T = T;
+  set_bounds(a, bounds);
   GB_CUDA_TRY(cudaMemsetAsync(queue, 0, sizeof(int32_t), s));
-  fn<<<blocks, NT, smem, s>>>(a, one_grid(grid, vis, ext_x, ext_y, pitch), (const float2*)gcf);
+  fn<<<blocks, NT, smem, s>>>(a, one_grid(grid, vis, ext_x, ext_y, pitch, bounds.n_vis),
+                              (const float2*)gcf);
   GB_CUDA_TRY(cudaGetLastError());
   return GB_OK;
 }
@@ -927,7 +990,8 @@ int launch_grid_tiled_tables(const Bundle* bundles, int n_bundles, const Item* i
 int launch_tiled_batch(bool grid_mode, int mode, int NT, size_t smem, int ctas_per_sm,
                        const Bundle* bundles, int n_bundles, const Item* items, const Rec* recs,
                        int32_t* queue, const ClassInfo* cls, int n_classes, int T,
-                       const GridPtrs& gp, const float* gcf, int stage, cudaStream_t s) {
+                       const GridPtrs& gp, const float* gcf, int stage,
+                       const TiledBounds& bounds, cudaStream_t s) {
   if (n_bundles <= 0) return GB_OK;
   TiledArgs a;
   a.bundles = bundles;
@@ -937,6 +1001,7 @@ int launch_tiled_batch(bool grid_mode, int mode, int NT, size_t smem, int ctas_p
   for (int c = 0; c < kMaxClasses; c++) a.cls[c] = c < n_classes ? cls[c] : ClassInfo{64, 1, 1, 1};
   a.n_bundles = n_bundles;
   a.T = T;
+  set_bounds(a, bounds);
   const int blocks = std::min(n_bundles, sm_count() * std::max(1, ctas_per_sm));
   // queue: the two work-queue heads (the grid kernel uses [0], degrid [1])
   GB_CUDA_TRY(cudaMemsetAsync(queue + (grid_mode ? 0 : 1), 0, sizeof(int32_t), s));
@@ -995,4 +1060,42 @@ extern "C" int gb_degrid_forward(gb_plan* P, const float* d_gcf, const float* d_
 extern "C" int gb_degrid_backward(gb_plan* P, const float* d_gcf, const float* d_pred_grad,
                                   float* d_grid_grad, void* stream) {
   return gb_grid_f32(P, d_pred_grad, d_gcf, d_grid_grad, stream);
+}
+
+// ---------------------------------------------------------------- bounds-checked build
+#ifdef GB_CHECKED
+__global__ void k_checked_selftest() {
+  // two indices out of range and one in range: no memory is touched
+  (void)gb_checked_index(5, 3);
+  (void)gb_checked_index(-1, 3);
+  (void)gb_checked_index(2, 3);
+}
+#endif
+
+extern "C" int gb_checked_violations(int64_t* out) {
+  if (!out) {
+    gb_set_error(GB_ERR_ARG, "gb_checked_violations: NULL argument");
+    return GB_ERR_ARG;
+  }
+#ifdef GB_CHECKED
+  unsigned long long v = 0, zero = 0;
+  GB_CUDA_TRY(cudaMemcpyFromSymbol(&v, g_check_violations, sizeof(v)));
+  GB_CUDA_TRY(cudaMemcpyToSymbol(g_check_violations, &zero, sizeof(zero)));
+  *out = (int64_t)v;
+#else
+  *out = -1;
+#endif
+  return GB_OK;
+}
+
+extern "C" int gb_checked_selftest(void) {
+#ifdef GB_CHECKED
+  k_checked_selftest<<<1, 1>>>();
+  GB_CUDA_TRY(cudaGetLastError());
+  GB_CUDA_TRY(cudaDeviceSynchronize());
+  return GB_OK;
+#else
+  gb_set_error(GB_ERR_ARG, "gb_checked_selftest: not a bounds-checked build");
+  return GB_ERR_ARG;
+#endif
 }

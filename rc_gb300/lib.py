@@ -133,6 +133,8 @@ SIGNATURES = {
     "gb_plan_device_status": (C.c_int, [_VP, C.POINTER(C.c_int32), _VP]),
     "gb_plan_set_stage": (C.c_int, [_VP, C.c_int32]),
     "gb_debug_fail_allocs": (C.c_int, [C.c_int32, C.c_int32]),
+    "gb_checked_violations": (C.c_int, [C.POINTER(C.c_int64)]),
+    "gb_checked_selftest": (C.c_int, []),
     "kern_fft": (C.c_int, [_VP, _VP]),
     "kern_ifft": (C.c_int, [_VP, _VP]),
     "gb_plan_export_index": (C.c_int, [_VP, _VP, _VP]),
@@ -202,15 +204,19 @@ class GbError(RuntimeError):
         self.code = code
 
 
-def load(path: str = LIB_PATH):
-    """Load librc_gb300.so (building it first if the sources are newer)."""
+def load(path: str = None):
+    """Load librc_gb300.so (building it first if the sources are newer).
+    RC_GB300_CHECKED=1 loads the bounds-checked variant instead."""
     global _lib
     if _lib is not None:
         return _lib
+    checked = os.environ.get("RC_GB300_CHECKED", "0") == "1"
+    if path is None:
+        path = os.path.join(HERE, "librc_gb300_checked.so") if checked else LIB_PATH
     if not os.path.exists(path) or os.environ.get("RC_GB300_AUTOBUILD", "1") == "1":
         try:
             from . import build as _b
-            _b.build()
+            _b.build(checked=checked)
         except Exception as e:  # no toolchain: a prebuilt library must exist
             if not os.path.exists(path):
                 raise RuntimeError(f"librc_gb300.so is missing and could not be built: {e}")
