@@ -53,8 +53,8 @@ static int batch_build(gb_batch* B, int32_t n, const gb_batch_member* m, cudaStr
   int rc;
   for (int i = 0; i < n; i++) {
     gb_plan* p = nullptr;
-    rc = gb_plan_create(&m[i].geo, m[i].n_vis, m[i].d_uvw, m[i].uvw_stride, m[i].d_plane,
-                        (void*)s, &p);
+    rc = plan_create(&m[i].geo, m[i].n_vis, m[i].d_uvw, m[i].uvw_stride, m[i].d_plane,
+                     (void*)s, false, &p);
     if (rc) return rc;
     B->members.push_back(p);
     if (p->T != B->members[0]->T || p->NT != B->members[0]->NT) {

@@ -449,7 +449,8 @@ static int build_plan(gb_plan* P, const gb_geometry* geo, int64_t n_vis, const d
   for (auto& h : items) h.grid = 0;
   std::vector<Item> it_sorted;
   std::vector<Bundle> bvec;
-  make_bundles(items, P->cls, P->n_classes, it_sorted, bvec);
+  // a batch member's work goes into the batch's own tables instead
+  if (P->own_work) make_bundles(items, P->cls, P->n_classes, it_sorted, bvec);
   P->n_items = (int)it_sorted.size();
   P->n_bundles = (int)bvec.size();
   // the items with their costs (any order), for batched launches
@@ -484,6 +485,12 @@ using namespace gb;
 extern "C" int gb_plan_create(const gb_geometry* geo, int64_t n_vis, const double* d_uvw,
                               int64_t uvw_stride, const int32_t* d_plane, void* stream,
                               gb_plan** out) {
+  return gb::plan_create(geo, n_vis, d_uvw, uvw_stride, d_plane, stream, true, out);
+}
+
+int gb::plan_create(const gb_geometry* geo, int64_t n_vis, const double* d_uvw,
+                    int64_t uvw_stride, const int32_t* d_plane, void* stream, bool own_work,
+                    gb_plan** out) {
   if (!out) {
     gb_set_error(GB_ERR_ARG, "gb_plan_create: NULL out");
     return GB_ERR_ARG;
@@ -519,8 +526,11 @@ extern "C" int gb_plan_create(const gb_geometry* geo, int64_t n_vis, const doubl
                  cap);
     return GB_ERR_ARG;
   }
+  int device = 0;
+  GB_CUDA_TRY(cudaGetDevice(&device));
   gb_plan* P = new gb_plan();
-  GB_CUDA_TRY(cudaGetDevice(&P->device));
+  P->own_work = own_work;
+  P->device = device;
   P->T = T;
   P->NT = NT;
   P->pcap = cap;

@@ -156,6 +156,7 @@ struct gb_plan {
   int64_t taps_paired = 0;  // taps of pieces that degridding can take in pairs
   int64_t gcf_len = 0;      // complex elements the planes' GCFs span
   int stage_pref = -1;      // GB_STAGE_*: forced staging form of degridding, or -1
+  bool own_work = true;     // false for a batch member: no launch tables of its own
   bool own_plane = true;
   std::vector<gb::HostItem> host_items;  // every item with its cost (grid slot 0)
   // TMA descriptors of the last degridded grid, one per thread-group class
@@ -186,6 +187,11 @@ int launch_degrid_tiled(gb_plan* plan, const float* gcf, const float* grid, floa
 size_t tiled_smem_grid(const ClassInfo* cls, int n_classes, int NT);
 size_t tiled_smem_degrid(const ClassInfo* cls, int n_classes, int NT);
 int tiled_max_smem();
+// gb_plan_create with own_work = false for a batch member: the plan computes
+// its records and items but no bundles (the batch builds its own tables).
+int plan_create(const gb_geometry* geo, int64_t n_vis, const double* d_uvw, int64_t uvw_stride,
+                const int32_t* d_plane, void* stream, bool own_work, gb_plan** out);
+
 // Array sizes behind a launch's pointers (used by the bounds-checked build).
 struct TiledBounds {
   int64_t n_recs, gcf_len, n_vis;
