@@ -15,16 +15,19 @@
 // lands on pixel (x0 + i, y0 + j) with i = (a - x0) mod P, so no two threads
 // ever touch the same pixel and the accumulation is a plain read-modify-write
 // with Kahan compensation carrying the rounding error of every addition in
-// a second accumulator.  At the end the group adds sum +
-// compensation into the global grid with float2 atomics, skipping pixels no
-// piece touched; atomics are needed only because neighbouring tiles'
-// overhangs and other items of the same tile overlap.
+// a second accumulator.  At the end the group adds the compensated sum
+// (sum - compensation) into the global grid with float2 atomics, skipping
+// pixels no piece touched; atomics are needed only because neighbouring
+// tiles' overhangs and other items of the same tile overlap.
 //
 // Degridding (D = G^H): each group stages its A x A grid region in shared
-// memory with coalesced loads, then each warp takes pieces, gathers the taps
-// from shared memory, multiplies by conj(GCF), sums with per-lane Kahan
-// compensation and a warp-shuffle reduction.  A visibility whose footprint was cut into
-// several pieces accumulates them with float2 atomics; otherwise a plain store.
+// memory (split rows by per-thread asynchronous copies, or plain rows by one
+// TMA copy or per-thread copies: gb_plan_set_stage), then sub-warps take
+// pieces, gather the taps (in pairs where the rows allow) from shared memory,
+// multiply by conj(GCF), sum each group of four steps by FMA chains into a
+// per-lane Kahan accumulator and reduce by warp shuffles.  A visibility whose
+// footprint was cut into several pieces accumulates them with float2 atomics;
+// otherwise a plain store.
 #include <algorithm>
 #include <cstring>
 #include <mutex>
