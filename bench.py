@@ -588,6 +588,7 @@ def our_arm_batch(args):
     s = torch.cuda.current_stream(dev)
     t0 = time.perf_counter()
     members, scale, supports, w_planes, wlo, whi = synth.config3(n_t=args.c3_nt)
+    n_ch_members = 64  # the channel grids come first, then the facets
     gen_s = time.perf_counter() - t0
     smax = int(supports.max())
     g64, g32, offs = Gm.generate(w_planes, supports, smax, scale / 2,
@@ -604,8 +605,31 @@ def our_arm_batch(args):
                            gcf_offsets=offs, w_range=(wlo, whi))
                       for u, m in zip(uvws, members)], **p)
 
-    params = dict(tile=args.tile or 24, threads=args.threads or 256,
-                  period_cap=args.cap or 40, bundles_per_cta=4)
+    # tunables: explicit flags, else the autotuner on the heaviest member (the
+    # highest channel: a 4096^2 grid and the largest w-supports), whose
+    # choice then runs the whole batch (every member shares the w-planes)
+    from rc_gb300 import autotune as AT
+    from rc_gb300.engine import Plan
+
+    explicit = {k: v for k, v in (("tile", args.tile), ("threads", args.threads),
+                                  ("period_cap", args.cap), ("bundles_per_cta", args.bpc)) if v}
+    tune_info = {"source": "flags" if explicit else "autotune"}
+    if explicit or args.no_tune:
+        params = dict(AT.DEFAULT, **explicit)
+        tune_info["source"] = "flags" if explicit else "defaults"
+    else:
+        k = n_ch_members - 1
+        m = members[k]
+
+        def make_plan(**p):
+            return Plan(uvws[k], scale=scale, grid_size=m.grid_size,
+                        grid_shape=(m.grid_size, m.grid_size), supports=supports,
+                        gcf_offsets=offs, w_range=(wlo, whi), **p)
+
+        t0 = time.perf_counter()
+        params, best_ms, table = AT.tune(make_plan, vis32[k], g32, grids[k])
+        tune_info.update(member=k, candidates=len(table), seconds=round(time.perf_counter() - t0, 2),
+                         best_ms=round(best_ms, 3))
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     B = make_batch(**params)
@@ -698,7 +722,8 @@ def our_arm_batch(args):
                                f"1024^2-4096^2), {n_vis} vis, 48 w-planes S 8-{smax}, one "
                                f"persistent launch per direction", "visibilities": n_vis,
                    "kept": st["kept"], "taps": st["taps"], "bundles": st["bundles"],
-                   "tuning": params, "graph": True, "generate_s": round(gen_s, 1),
+                   "tuning": dict(params, **tune_info), "graph": True,
+                   "generate_s": round(gen_s, 1),
                    "l2": "flushed (256 MiB write) before every step"},
         "roofline": {"bound": "hbm", "kernel": dom[0], "achieved": round(achieved, 1),
                      "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
