@@ -88,7 +88,7 @@ def build(force: bool = False, ptxas_verbose: bool = False, verbose: bool = Fals
     libdir = os.path.join(cuda_home(), "lib64")
     tmp = lib_out + ".tmp"
     cmd = [cc] + ARCH + ["-shared", "-o", tmp] + objs + [
-        "-L", libdir, "-lcufft", "-Xlinker", "-rpath," + libdir]
+        "-L", libdir, "-lcufft", "-lpthread", "-Xlinker", "-rpath," + libdir]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

@@ -12,7 +12,10 @@
 // and geometry travel in a __grid_constant__ kernel parameter block, so a
 // batched call is a memset plus one launch and captures into a CUDA graph.
 #include <algorithm>
+#include <atomic>
 #include <cstring>
+#include <string>
+#include <thread>
 #include <vector>
 
 #include "gb_common.cuh"
@@ -49,19 +52,72 @@ static void free_batch(gb_batch* B) {
   delete B;
 }
 
+// The members' plans, built side by side on host threads (each with its own
+// stream, ordered after the work already queued on the caller's stream): a
+// plan's host part (bins, items) is most of its time.  Returns the first
+// member's error, with its message, on the calling thread.
+static int build_members(gb_batch* B, int32_t n, const gb_batch_member* m, cudaStream_t s) {
+  int dev = 0;
+  GB_CUDA_TRY(cudaGetDevice(&dev));
+  cudaEvent_t ready;
+  GB_CUDA_TRY(cudaEventCreateWithFlags(&ready, cudaEventDisableTiming));
+  const cudaError_t er = cudaEventRecord(ready, s);
+  if (er != cudaSuccess) {
+    cudaEventDestroy(ready);
+    GB_CUDA_TRY(er);
+  }
+  std::vector<gb_plan*> plans(n, nullptr);
+  std::vector<int> rcs(n, GB_OK);
+  std::vector<std::string> errs(n);
+  std::atomic<int> next{0};
+  auto work = [&]() {
+    cudaStream_t ws = nullptr;
+    const bool ok = cudaSetDevice(dev) == cudaSuccess &&
+                    cudaStreamCreateWithFlags(&ws, cudaStreamNonBlocking) == cudaSuccess &&
+                    cudaStreamWaitEvent(ws, ready, 0) == cudaSuccess;
+    for (int i; (i = next++) < n;) {
+      if (!ok) {
+        rcs[i] = GB_ERR_CUDA;
+        errs[i] = "gb_batch_create: could not set up a worker stream";
+        continue;
+      }
+      rcs[i] = plan_create(&m[i].geo, m[i].n_vis, m[i].d_uvw, m[i].uvw_stride, m[i].d_plane,
+                           (void*)ws, false, &plans[i]);
+      if (rcs[i]) errs[i] = gb_last_error();
+    }
+    if (ws) cudaStreamDestroy(ws);
+  };
+  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+  const int nthreads = (int)std::min<unsigned>({(unsigned)n, hw, 16u});
+  std::vector<std::thread> pool;
+  for (int t = 1; t < nthreads; t++) pool.emplace_back(work);
+  work();
+  for (auto& t : pool) t.join();
+  cudaEventDestroy(ready);
+  int first = -1;
+  for (int i = 0; i < n; i++)
+    if (rcs[i] && first < 0) first = i;
+  if (first >= 0) {
+    for (gb_plan* p : plans)
+      if (p) gb_plan_destroy(p);
+    // errs holds "[code] message": keep the message
+    const std::string& e = errs[first];
+    const size_t k = e.find("] ");
+    gb_set_error(rcs[first], "%s", k == std::string::npos ? e.c_str() : e.c_str() + k + 2);
+    return rcs[first];
+  }
+  B->members = std::move(plans);
+  return GB_OK;
+}
+
 static int batch_build(gb_batch* B, int32_t n, const gb_batch_member* m, cudaStream_t s) {
-  int rc;
-  for (int i = 0; i < n; i++) {
-    gb_plan* p = nullptr;
-    rc = plan_create(&m[i].geo, m[i].n_vis, m[i].d_uvw, m[i].uvw_stride, m[i].d_plane,
-                     (void*)s, false, &p);
-    if (rc) return rc;
-    B->members.push_back(p);
+  int rc = build_members(B, n, m, s);
+  if (rc) return rc;
+  for (gb_plan* p : B->members)
     if (p->T != B->members[0]->T || p->NT != B->members[0]->NT) {
       gb_set_error(GB_ERR_ARG, "gb_batch_create: members need the same tile and threads");
       return GB_ERR_ARG;
     }
-  }
   B->T = B->members[0]->T;
   B->NT = B->members[0]->NT;
   // union of the thread-group classes, by group width
