@@ -284,6 +284,7 @@ extern "C" int gb_grid_f32_noalloc(const gb_geometry* geo, int64_t n_vis, const 
     q.S = S;
     q.k = (S + cap - 1) / cap;
     q.P = (S + q.k - 1) / q.k;
+    if (q.k > 1 && !(S & 1) && (q.P & 1) && q.P < cap) q.P++;  // even-width pieces
     q.gcf_off = geo->gcf_offsets[p];
     gcf_len = std::max<int64_t>(gcf_len, q.gcf_off + (int64_t)GB_PHASES * S * S);
     kmax = q.k > kmax ? q.k : kmax;

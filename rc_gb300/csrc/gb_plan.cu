@@ -242,6 +242,9 @@ static int build_plan(gb_plan* P, const gb_geometry* geo, int64_t n_vis, const d
     q.S = geo->supports[p];
     q.k = (q.S + P->pcap - 1) / P->pcap;
     q.P = (q.S + q.k - 1) / q.k;
+    // an even support is cut into even-width pieces (the last one narrower),
+    // so degridding can take every piece's taps in pairs
+    if (q.k > 1 && !(q.S & 1) && (q.P & 1) && q.P < P->pcap) q.P++;
     q.gcf_off = geo->gcf_offsets[p];
     P->gcf_len = std::max<int64_t>(P->gcf_len, q.gcf_off + (int64_t)GB_PHASES * q.S * q.S);
     periods.push_back(q.P);

@@ -111,6 +111,8 @@ def expected_auto_stage(P, c, cap):
         S = int(S)
         k = (S + cap - 1) // cap
         Pp = (S + k - 1) // k
+        if k > 1 and S % 2 == 0 and Pp % 2 == 1 and Pp < cap:
+            Pp += 1  # even supports are cut into even-width pieces
         for ky in range(k):
             for kx in range(k):
                 if kx * Pp >= S or ky * Pp >= S:
