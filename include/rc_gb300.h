@@ -80,9 +80,11 @@ const char *gb_version(void);
 /* replaces MS6/kernel/gpu/gridding/kern_scatter_gpu1.cpp:21-40 */
 int kern_scatter_gpu1(double scale, int32_t grid_size, int32_t margin_size,
                       buffer_t *vis, buffer_t *gcf, buffer_t *uvg);
+#ifndef GB_MS5_ABI /* the MS5 variant binds its own kern_scatter (rc_gb300_ms5.h) */
 /* replaces MS6/kernel/cpu/gridding/scatter1.cpp:9-20 (the CPU slot; runs on the GPU) */
 int kern_scatter(double scale, int32_t grid_size, int32_t margin_size,
                  buffer_t *vis, buffer_t *gcf, buffer_t *uvg);
+#endif
 /* replaces MS6/kernel/nvidia/gridder/halide_api.cu:4-29, in the form the
  * Haskell side binds it (MS6/programs/Kernel/Gridder.hs:70: three scalars,
  * margin included); same semantics as kern_scatter_gpu1. */
@@ -387,7 +389,9 @@ int gb_grid_to_image_f64(const double *d_grid, const double *d_taper, int32_t n,
  * rc_gb300/csrc/gb_imaging.cu.  Returns GB_ERR_FFT_SIZE for mismatched or
  * unsupported sizes, GB_ERR_ARG for a malformed buffer.  Synchronous. */
 #define GB_ERR_FFT_SIZE (-666) /* MS6/kernel/cpu/gridding/fft1.cpp:38,52 */
+#ifndef GB_MS5_ABI /* the MS5 variant binds its own kern_fft (rc_gb300_ms5.h) */
 int kern_fft(buffer_t *image, buffer_t *uvg_herm);
+#endif
 int kern_ifft(buffer_t *uvg, buffer_t *img_shifted);
 
 /* GCF choice for a w-region [w0, w1] among precomputed GCFs of nominal w

@@ -23,6 +23,10 @@ LIB = os.path.join(HERE, "librc_gb300.so")
 # the bounds-checked variant (-DGB_CHECKED), built on request
 LIB_CHECKED = os.path.join(HERE, "librc_gb300_checked.so")
 BUILD_CHECKED = os.path.join(HERE, "_build_checked")
+# the MS5 binding variant (-DGB_MS5_ABI: MS5's kern_scatter and kern_fft,
+# include/rc_gb300_ms5.h), built on request
+LIB_MS5 = os.path.join(HERE, "librc_gb300_ms5.so")
+BUILD_MS5 = os.path.join(HERE, "_build_ms5")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -55,10 +59,12 @@ def up_to_date(lib: str = LIB) -> bool:
 
 
 def build(force: bool = False, ptxas_verbose: bool = False, verbose: bool = False,
-          checked: bool = False) -> str:
+          checked: bool = False, ms5: bool = False) -> str:
     """Build the library; checked=True builds the bounds-checked variant
-    (librc_gb300_checked.so, -DGB_CHECKED) instead."""
-    lib_out, build_dir = (LIB_CHECKED, BUILD_CHECKED) if checked else (LIB, BUILD)
+    (librc_gb300_checked.so, -DGB_CHECKED), ms5=True the MS5 binding variant
+    (librc_gb300_ms5.so, -DGB_MS5_ABI) instead."""
+    lib_out, build_dir = ((LIB_CHECKED, BUILD_CHECKED) if checked else
+                          (LIB_MS5, BUILD_MS5) if ms5 else (LIB, BUILD))
     if not force and up_to_date(lib_out):
         return lib_out
     os.makedirs(build_dir, exist_ok=True)
@@ -67,6 +73,8 @@ def build(force: bool = False, ptxas_verbose: bool = False, verbose: bool = Fals
                     "--expt-relaxed-constexpr"]
     if checked:
         flags += ["-DGB_CHECKED"]
+    if ms5:
+        flags += ["-DGB_MS5_ABI"]
     if ptxas_verbose:
         flags += ["-Xptxas", "-v"]
 

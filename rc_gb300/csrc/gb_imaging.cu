@@ -21,6 +21,7 @@
 #include <tuple>
 
 #include "gb_common.cuh"
+#include "rc_gb300_ms5.h"
 #include "gb_runtime.cuh"
 
 namespace gb {
@@ -208,7 +209,8 @@ static int grid_to_image(const typename Cx<R>::T* g, const R* t, int n, typename
 // so it sits about 1e-8 (relative) from these exact transforms.
 constexpr int kFftSizeError = -666;  // fft1.cpp:38, 52
 
-__global__ void k_ifft_prep(const double2* __restrict__ g, int n, double2* __restrict__ a) {
+__global__ void k_ifft_prep(const double2* __restrict__ g, int n, double herm_scale,
+                            double2* __restrict__ a) {
   const int h = n / 2;
   const int64_t total = (int64_t)(h + 1) * n;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
@@ -217,7 +219,7 @@ __global__ void k_ifft_prep(const double2* __restrict__ g, int n, double2* __res
     const int ua = half_shift(u, n), vb = half_shift(v, n);
     const double2 p = g[(int64_t)vb * n + ua];
     const double2 m = g[(int64_t)(n - 1 - vb) * n + (n - 1 - ua)];
-    a[i] = make_double2((p.x + m.x) / 2, (p.y - m.y) / 2);
+    a[i] = make_double2((p.x + m.x) * herm_scale, (p.y - m.y) * herm_scale);
   }
 }
 
@@ -236,10 +238,10 @@ __global__ void k_ifft_complete(const double2* __restrict__ a, int n, double2* _
   }
 }
 
-__global__ void k_ifft_out(const double2* __restrict__ t, int n, double* __restrict__ out) {
+__global__ void k_ifft_out(const double2* __restrict__ t, int n, double rn,
+                           double* __restrict__ out) {
   const int h = n / 2;
   const int64_t total = (int64_t)n * n;
-  const double rn = 1.0 / n;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
        i += (int64_t)gridDim.x * blockDim.x) {
     const int y = (int)(i / n), x = (int)(i - (int64_t)y * n);
@@ -350,9 +352,16 @@ static int fft_size(const buffer_t* img, const buffer_t* uvg, const char* who) {
 
 using namespace gb;
 
-extern "C" int kern_ifft(buffer_t* uvg, buffer_t* img) {
-  const int n = fft_size(img, uvg, "kern_ifft");
+// The inverse pipeline with its two scale factors: MS6's kern_ifft hermitises
+// with 1/2 and divides the image by n; MS5's kern_fft does neither.
+static int ifft_host(buffer_t* uvg, buffer_t* img, const char* who, double herm_scale,
+                     bool scale_by_n, int only_size) {
+  const int n = fft_size(img, uvg, who);
   if (n < 0) return n;
+  if (only_size && n != only_size) {
+    gb_set_error(GB_ERR_ARG, "%s: the grid must be %d x %d", who, only_size, only_size);
+    return GB_ERR_ARG;
+  }
   int rc;
   cudaStream_t s;
   if ((rc = stage_stream(&s))) return rc;
@@ -364,14 +373,14 @@ extern "C" int kern_ifft(buffer_t* uvg, buffer_t* img) {
   double2* a = (double2*)d1;
   GB_CUDA_TRY(cudaMemcpy2DAsync(g, (size_t)n * 16, uvg->host, (size_t)uvg->stride[2] * 8,
                                 (size_t)n * 16, n, cudaMemcpyHostToDevice, s));
-  k_ifft_prep<<<blocks_nn((int64_t)(n / 2 + 1) * n), 256, 0, s>>>(g, n, a);
+  k_ifft_prep<<<blocks_nn((int64_t)(n / 2 + 1) * n), 256, 0, s>>>(g, n, herm_scale, a);
   GB_CUDA_TRY(cudaGetLastError());
   if ((rc = exec_1d(a, n, n / 2 + 1, false, s))) return rc;
   k_ifft_complete<<<blocks_nn((int64_t)cells), 256, 0, s>>>(a, n, g);
   GB_CUDA_TRY(cudaGetLastError());
   if ((rc = exec_1d(g, n, n, true, s))) return rc;
   double* out = (double*)d1;
-  k_ifft_out<<<blocks_nn((int64_t)cells), 256, 0, s>>>(g, n, out);
+  k_ifft_out<<<blocks_nn((int64_t)cells), 256, 0, s>>>(g, n, scale_by_n ? 1.0 / n : 1.0, out);
   GB_CUDA_TRY(cudaGetLastError());
   GB_CUDA_TRY(cudaMemcpy2DAsync(img->host, (size_t)img->stride[1] * 8, out, (size_t)n * 8,
                                 (size_t)n * 8, n, cudaMemcpyDeviceToHost, s));
@@ -379,6 +388,19 @@ extern "C" int kern_ifft(buffer_t* uvg, buffer_t* img) {
   return GB_OK;
 }
 
+extern "C" int kern_ifft(buffer_t* uvg, buffer_t* img) {
+  return ifft_host(uvg, img, "kern_ifft", 0.5, true, 0);
+}
+
+#ifdef GB_MS5_ABI
+// MS5's kern_fft (MS5/programs/Kernel/FFT.hs:15-16, generated by
+// MS5/kernel/cpu/gridding/fft.cpp:540-605): grid -> image, 2048 x 2048 only,
+// the grid hermitised without the 1/2 and the image not divided by n, i.e.
+// 2 n times MS6's kern_ifft.
+extern "C" int kern_fft(buffer_t* uvg, buffer_t* img) {
+  return ifft_host(uvg, img, "kern_fft", 1.0, false, 2048);
+}
+#else
 extern "C" int kern_fft(buffer_t* img, buffer_t* uvg) {
   const int n = fft_size(img, uvg, "kern_fft");
   if (n < 0) return n;
@@ -404,6 +426,7 @@ extern "C" int kern_fft(buffer_t* img, buffer_t* uvg) {
   GB_CUDA_TRY(cudaStreamSynchronize(s));
   return GB_OK;
 }
+#endif  // GB_MS5_ABI
 
 extern "C" int gb_image_to_grid_f32(const float* d_image, const float* d_taper, int32_t n,
                                     float* d_grid, void* stream) {

@@ -14,6 +14,7 @@
 #include "gb_common.cuh"
 #include "gb_plan.cuh"
 #include "gb_runtime.cuh"
+#include "rc_gb300_ms5.h"
 
 namespace gb {
 
@@ -354,11 +355,26 @@ extern "C" int kern_scatter_gpu1(double scale, int32_t grid_size, int32_t margin
                         margin_size, vis, gcf, uvg);
 }
 
+#ifdef GB_MS5_ABI
+// MS5's gridder binding (MS5/programs/Kernel/Gridder.hs:28-35; the kernel is
+// generated by MS5/kernel/cpu/gridding/scatter.cpp:10-121): no margin argument
+// and the GCF size fixed at 16.  Its bounds, min .. min + extent - 16 - 1, are
+// the MS6 rule with the margin equal to the support.
+extern "C" int kern_scatter(double scale, int32_t grid_size, buffer_t* vis, buffer_t* gcf,
+                            buffer_t* uvg) {
+  if (gcf && check_size(gcf) != 16) {
+    gb_set_error(GB_ERR_ARG, "kern_scatter: the GCF must be (2,16,16,64) (MS5/scatter.cpp:36-41)");
+    return GB_ERR_ARG;
+  }
+  return compat_scatter("kern_scatter", GB_ERR_ARG, scale, grid_size, 16, vis, gcf, uvg);
+}
+#else
 extern "C" int kern_scatter(double scale, int32_t grid_size, int32_t margin_size, buffer_t* vis,
                             buffer_t* gcf, buffer_t* uvg) {
   return compat_scatter("kern_scatter", GB_ERR_SCATTER_SIZE, scale, grid_size, margin_size, vis,
                         gcf, uvg);
 }
+#endif
 
 extern "C" int nvGridder(double scale, int32_t grid_size, int32_t margin_size, buffer_t* vis,
                          buffer_t* gcf, buffer_t* uvg) {

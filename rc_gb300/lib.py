@@ -229,6 +229,38 @@ def load(path: str = None):
     return L
 
 
+# MS5's two bindings that differ from MS6's (include/rc_gb300_ms5.h)
+MS5_SIGNATURES = dict(SIGNATURES)
+MS5_SIGNATURES["kern_scatter"] = (C.c_int, [C.c_double, C.c_int32, _BP, _BP, _BP])
+MS5_SIGNATURES["kern_fft"] = (C.c_int, [_VP, _VP])
+
+_lib_ms5 = None
+
+
+def load_ms5():
+    """Load librc_gb300_ms5.so, the MS5 binding variant (built first if the
+    sources are newer).  Its own handle: the MS6 library can be loaded in the
+    same process."""
+    global _lib_ms5
+    if _lib_ms5 is not None:
+        return _lib_ms5
+    path = os.path.join(HERE, "librc_gb300_ms5.so")
+    if not os.path.exists(path) or os.environ.get("RC_GB300_AUTOBUILD", "1") == "1":
+        try:
+            from . import build as _b
+            _b.build(ms5=True)
+        except Exception as e:
+            if not os.path.exists(path):
+                raise RuntimeError(f"librc_gb300_ms5.so is missing and could not be built: {e}")
+    L = C.CDLL(path)
+    for name, (res, args) in MS5_SIGNATURES.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib_ms5 = L
+    return L
+
+
 def last_error() -> str:
     return load().gb_last_error().decode(errors="replace")
 
