@@ -241,6 +241,41 @@ def _gcf_host(ob):
 
 
 # ---------------------------------------------------------------- our arm
+def abi_e2e(ob, steps, warmup):
+    """Config 1 through the reference's own host-buffer symbols, the way the
+    MS6 Haskell gridder calls them (MS6/programs/Kernel/Gridder.hs:58-71,
+    Degrid.hs:146-155): one kern_scatter_gpu1 and one kern_degrid_gpu1 per
+    (tile, w-bin), and config 1 has one of each.  FP64 5-double records, the
+    7 x 7 PSWF in S = 8, a complex128 grid in pageable host memory; every copy
+    is inside the call.  Each step grids into a zeroed grid (zeroed outside the
+    timer) and degrids from the result.  Returns the e2e object."""
+    from rc_gb300 import compat
+    from rc_gb300 import gcf as Gm
+
+    vis5 = ob.vis5()
+    S, G = 8, ob.grid_size
+    gcf = Gm.pswf_uv_gcf(S, 7)
+    grid = np.zeros((G, G), np.complex128)
+    out = np.zeros_like(vis5)
+    times = []
+    for i in range(warmup + steps):
+        grid.fill(0)
+        t0 = time.perf_counter()
+        rc1 = compat.call_scatter("kern_scatter_gpu1", ob.scale, G, S, vis5, gcf, grid)
+        rc2 = compat.call_degrid("kern_degrid_gpu1", ob.scale, G, S, gcf, grid, vis5, out)
+        t1 = time.perf_counter()
+        assert rc1 == 0 and rc2 == 0, (rc1, rc2)
+        if i >= warmup:
+            times.append(t1 - t0)
+    t = float(np.mean(times))
+    n, gcf_b, grid_b = ob.n, gcf.size * 16, G * G * 16
+    return {"value": round(n / t / 1e6, 3), "unit": "Mvis/s", "ms_per_step": round(1e3 * t, 3),
+            "h2d_bytes_per_step": 2 * (40 * n + gcf_b + grid_b),
+            "d2h_bytes_per_step": grid_b + 40 * n,
+            "path": "kern_scatter_gpu1 + kern_degrid_gpu1 on pageable host buffer_t (FP64), "
+                    "host wall clock per step, mean of K after W"}
+
+
 def our_arm(args):
     import torch
 
@@ -517,6 +552,7 @@ def our_arm(args):
                 lat.append(t0e.elapsed_time(t1e))
         e2e_lat = float(np.median(lat))
     e2e_mvis = world * ob.n / (e2e_ms * 1e-3) / 1e6 if e2e_ms else float("nan")
+    abi = abi_e2e(ob, args.steps, args.warmup) if args.config == "c1" and not args.quick else None
     h2d = h_vis.numel() * 8 + h_model.numel() * 8
     d2h = h_grid[0].numel() * 8 + h_pred[0].numel() * 8
 
@@ -560,6 +596,7 @@ def our_arm(args):
                     "timing": "K steps pipelined (double-buffered, copies on their own "
                               "streams) between two events, / K",
                     "single_step_latency_ms": round(e2e_lat, 3) if e2e_lat else None},
+            "e2e_reference_abi": abi,
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
             "gpu_launches": 2 * args.steps,
