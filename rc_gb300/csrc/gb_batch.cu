@@ -38,6 +38,7 @@ struct gb_batch {
   int n_items = 0, n_bundles = 0;
   int64_t kept = 0, taps = 0, taps_paired = 0;
   int64_t gcf_len = 0;
+  gb::DfScratch df;  // FP64 degridding scratch, shared by the members' launches
 };
 
 using namespace gb;
@@ -49,6 +50,7 @@ static void free_batch(gb_batch* B) {
   cudaFree(B->d_items);
   cudaFree(B->d_bundles);
   cudaFree(B->d_queue);
+  B->df.release();
   delete B;
 }
 
@@ -339,6 +341,12 @@ extern "C" int gb_batch_degrid_f64(gb_batch* B, const double* d_gcf, const doubl
     gb_set_error(GB_ERR_ARG, "gb_batch_degrid_f64: bad argument");
     return GB_ERR_ARG;
   }
+  // the scratch at the largest member's size first: the members' launches
+  // then reuse it in stream order without reallocating under a running kernel
+  int64_t cells = 0;
+  for (const gb_plan* p : B->members) cells = std::max(cells, (int64_t)p->dev.ext_x * p->dev.ext_y);
+  int rc0;
+  if ((rc0 = df_reserve(B->df, cells, B->gcf_len))) return rc0;
   for (size_t i = 0; i < B->members.size(); i++) {
     if (!B->members[i]->dev.n_vis) continue;
     if (!d_grids[i] || !d_preds[i]) {
@@ -346,7 +354,7 @@ extern "C" int gb_batch_degrid_f64(gb_batch* B, const double* d_gcf, const doubl
       return GB_ERR_ARG;
     }
     const int rc = launch_degrid_plain64(B->members[i], d_gcf, d_grids[i], d_preds[i], mode,
-                                         (cudaStream_t)stream);
+                                         B->df, (cudaStream_t)stream);
     if (rc) return rc;
   }
   return GB_OK;

@@ -11,6 +11,8 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <algorithm>
+
 #include "gb_common.cuh"
 #include "gb_plan.cuh"
 #include "gb_runtime.cuh"
@@ -73,6 +75,156 @@ __device__ __forceinline__ double2 warp_gather64(const double2* __restrict__ bas
   return make_double2(ar, ai);
 }
 
+// ---------------------------------------------------------------- double-float gather
+// The FP64 pipe of this part runs at a small fraction of its FP32 rate
+// (nominal 1.25 TFLOP/s FP64 for the whole GPU), so the FP64 degridders do
+// their tap arithmetic in double-float on the FP32 pipe.  Each operand array
+// is scaled by the power of two that brings its largest magnitude into [1, 2)
+// and every double x is held as hi + lo: hi = x rounded to 24 significant
+// bits, lo = the remainder rounded to 24 (x to 2^-48 relative).  A product is
+// hi*hi with its exact FMA error plus the hi*lo cross terms (lo*lo, under
+// 2^-48 of the product, is left out); the running sums are TwoSum pairs (hi
+// sum, low-order sum), so each addition errs by about 2^-48 of the running sum,
+// as in a 48-bit floating-point format (FP64: 2^-53).  Scaled values below
+// 2^-74 lose their low part and those below 2^-126 are dropped (an absolute
+// error under 2^-98 of the array's largest value).  An Inf, a NaN or a
+// subnormal in either array sends the launch down the native FP64 loop
+// instead, so that those propagate as FP64 arithmetic would.
+
+constexpr int kExpNonFinite = 0x7FF;
+
+// Largest biased exponent field over rows x row doubles (rows `pitch` doubles
+// apart), max-ed into *out, which the caller zeroes.  A subnormal counts as
+// kExpNonFinite too: the split would drop it, so the native loop takes it.
+__global__ void k_max_exponent(const double* __restrict__ x, int64_t rows, int64_t row,
+                               int64_t pitch, int* __restrict__ out) {
+  int m = 0;
+  for (int64_t r = blockIdx.y; r < rows; r += gridDim.y) {
+    const unsigned long long* xr = (const unsigned long long*)(x + r * pitch);
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < row;
+         c += (int64_t)gridDim.x * blockDim.x) {
+      const unsigned long long b = xr[c];
+      const int e = (int)((b >> 52) & 0x7FF);
+      m = max(m, e == 0 && (b & 0xFFFFFFFFFFFFFull) ? kExpNonFinite : e);
+    }
+  }
+  m = __reduce_max_sync(0xffffffffu, m);
+  if ((threadIdx.x & 31) == 0 && m) atomicMax(out, m);
+}
+
+// The scale exponent of an array from its largest exponent field: the array
+// is multiplied by 2^-k (k = 0 for an array of zeros).
+__device__ __forceinline__ int df_scale_exp(int e) { return e > 0 && e < kExpNonFinite ? e - 1023 : 0; }
+
+// x * 2^-k as (hi, lo) floats from x's bit pattern, no FP64 arithmetic: hi =
+// the scaled x rounded to 24 significant bits (a carry out of the mantissa
+// moves into the exponent field), lo = the remaining 29-bit signed remainder
+// rounded to 24 bits.
+__device__ __forceinline__ float2 df_split(unsigned long long b, int k) {
+  const unsigned hi32 = (unsigned)(b >> 32), lo32 = (unsigned)b;
+  const int e = (int)((hi32 >> 20) & 0x7FF);
+  const int fe = e - k - 896;  // biased float exponent of the scaled value (1023 - 127 = 896)
+  if (e == 0 || fe <= 0) return make_float2(0.f, 0.f);
+  const unsigned sign = hi32 & 0x80000000u;
+  const unsigned top = ((hi32 & 0xFFFFFu) << 3) | (lo32 >> 29);  // mantissa bits 51..29
+  const unsigned up = (lo32 >> 28) & 1u;                          // bit 28: round up
+  const float hi = __uint_as_float(sign | ((((unsigned)fe << 23) | top) + up));
+  // mantissa bits 28..0, less 2^29 when hi was rounded up, are worth
+  // rem * 2^(fe - 127 - 52) in magnitude
+  float lo = 0.f;
+  if (fe > 52) {
+    const int rem = (int)(lo32 & 0x1FFFFFFFu) - (int)(up << 29);
+    lo = __int2float_rn(rem) * __uint_as_float((unsigned)(fe - 52) << 23);
+  }
+  return make_float2(hi, __uint_as_float(__float_as_uint(lo) ^ sign));
+}
+
+// out[r * row + c] = split of x[r * pitch + c] under the scale of exps[which];
+// nothing when either array of the launch holds an Inf or NaN.
+__global__ void k_df_split(const double* __restrict__ x, int64_t rows, int64_t row, int64_t pitch,
+                           const int* __restrict__ exps, int which, float2* __restrict__ out) {
+  if (exps[0] == kExpNonFinite || exps[1] == kExpNonFinite) return;
+  const int k = df_scale_exp(exps[which]);
+  for (int64_t r = blockIdx.y; r < rows; r += gridDim.y) {
+    const unsigned long long* xr = (const unsigned long long*)(x + r * pitch);
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < row;
+         c += (int64_t)gridDim.x * blockDim.x)
+      out[r * row + c] = df_split(xr[c], k);
+  }
+}
+
+// s + p into the pair (s, c): s the rounded sum, c += its exact rounding error.
+__device__ __forceinline__ void two_sum_acc(float& s, float& c, float p) {
+  const float t = __fadd_rn(s, p);
+  const float bp = __fsub_rn(t, s);
+  const float e = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bp)), __fsub_rn(p, bp));
+  s = t;
+  c = __fadd_rn(c, e);
+}
+
+// acc += a * b (CONJ: a * conj(b)) for complex double-floats laid out
+// (re hi, re lo, im hi, im lo); acc = (re sum, im sum, re low-order, im low-order).
+template <bool CONJ>
+__device__ __forceinline__ void df_cmac(const float4 a, float4 b, float4& acc) {
+  if (CONJ) {
+    b.z = -b.z;
+    b.w = -b.w;
+  }
+  const float p1 = __fmul_rn(a.x, b.x), e1 = __fmaf_rn(a.x, b.x, -p1);  // re re
+  const float p2 = __fmul_rn(a.z, b.z), e2 = __fmaf_rn(a.z, b.z, -p2);  // im im
+  const float p3 = __fmul_rn(a.x, b.z), e3 = __fmaf_rn(a.x, b.z, -p3);  // re im
+  const float p4 = __fmul_rn(a.z, b.x), e4 = __fmaf_rn(a.z, b.x, -p4);  // im re
+  float lr = __fmaf_rn(a.x, b.y, __fmaf_rn(a.y, b.x, __fsub_rn(e1, e2)));
+  lr = __fmaf_rn(-a.z, b.w, __fmaf_rn(-a.w, b.z, lr));
+  float li = __fmaf_rn(a.x, b.w, __fmaf_rn(a.y, b.z, __fadd_rn(e3, e4)));
+  li = __fmaf_rn(a.z, b.y, __fmaf_rn(a.w, b.x, li));
+  acc.z = __fadd_rn(acc.z, lr);
+  acc.w = __fadd_rn(acc.w, li);
+  two_sum_acc(acc.x, acc.z, p1);
+  two_sum_acc(acc.x, acc.z, -p2);
+  two_sum_acc(acc.y, acc.w, p3);
+  two_sum_acc(acc.y, acc.w, p4);
+}
+
+template <bool CONJ>
+__device__ __forceinline__ float4 warp_gather_df(const float4* __restrict__ base, int64_t pitch,
+                                                 const float4* __restrict__ g, int S, int lane) {
+  float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+  TapWalk w(S, lane);
+  for (; w.j < S; w.next())
+    df_cmac<CONJ>(base[(int64_t)w.j * pitch + w.i], __ldg(g + w.j * S + w.i), acc);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const float sr = __shfl_xor_sync(0xffffffffu, acc.x, o);
+    const float si = __shfl_xor_sync(0xffffffffu, acc.y, o);
+    acc.z = __fadd_rn(acc.z, __shfl_xor_sync(0xffffffffu, acc.z, o));
+    acc.w = __fadd_rn(acc.w, __shfl_xor_sync(0xffffffffu, acc.w, o));
+    two_sum_acc(acc.x, acc.z, sr);
+    two_sum_acc(acc.y, acc.w, si);
+  }
+  return acc;
+}
+
+// A double-float sum back to FP64, times 2^kt.
+__device__ __forceinline__ double2 df_to_double(float4 a, int kt) {
+  return make_double2(ldexp((double)a.x + (double)a.z, kt), ldexp((double)a.y + (double)a.w, kt));
+}
+
+// Lane l of a warp indexes visibility t0 + l once; the warp then takes the
+// visibilities one by one, fetching each index from its lane.
+struct LaneIndex {
+  int32_t x0, y0, phase, keep, plane;
+  __device__ __forceinline__ LaneIndex from(int j) const {
+    LaneIndex r;
+    r.x0 = __shfl_sync(0xffffffffu, x0, j);
+    r.y0 = __shfl_sync(0xffffffffu, y0, j);
+    r.phase = __shfl_sync(0xffffffffu, phase, j);
+    r.keep = __shfl_sync(0xffffffffu, keep, j);
+    r.plane = __shfl_sync(0xffffffffu, plane, j);
+    return r;
+  }
+};
+
 // ---------------------------------------------------------------- single GCF (ABI form)
 struct SingleGeo {
   double scale;
@@ -81,108 +233,227 @@ struct SingleGeo {
   int64_t pitch;  // complex elements per grid row
 };
 
+__device__ __forceinline__ LaneIndex single_index(const double* __restrict__ vis5, int64_t t,
+                                                  int64_t n, const SingleGeo& geo) {
+  LaneIndex li{0, 0, 0, 0, 0};
+  if (t < n) {
+    const VisIndex ix = vis_index(vis5[5 * t], vis5[5 * t + 1], geo.scale, geo.grid_size, geo.S,
+                                  geo.margin, geo.min_x, geo.min_y, geo.ext_x, geo.ext_y);
+    li.x0 = ix.x0 - geo.min_x;
+    li.y0 = ix.y0 - geo.min_y;
+    li.phase = ix.phase;
+    li.keep = ix.keep;
+  }
+  return li;
+}
+
 __global__ void k_scatter_single64(int64_t n, const double* __restrict__ vis5,
                                    const double2* __restrict__ gcf, double2* __restrict__ grid,
                                    SingleGeo geo) {
   const int lane = threadIdx.x & 31;
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
-  for (int64_t t = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5); t < n;
-       t += warps) {
-    const double* r = vis5 + 5 * t;
-    const VisIndex ix = vis_index(r[0], r[1], geo.scale, geo.grid_size, geo.S, geo.margin,
-                                  geo.min_x, geo.min_y, geo.ext_x, geo.ext_y);
-    if (!ix.keep) continue;
-    double2* base = grid + (int64_t)(ix.y0 - geo.min_y) * geo.pitch + (ix.x0 - geo.min_x);
-    warp_scatter64(base, geo.pitch, gcf + (int64_t)ix.phase * geo.S * geo.S, geo.S, r[3], r[4],
-                   lane);
+  for (int64_t t0 = 32 * (blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5)); t0 < n;
+       t0 += 32 * warps) {
+    const LaneIndex mine = single_index(vis5, t0 + lane, n, geo);
+    const int m = (int)min((int64_t)32, n - t0);
+    for (int j = 0; j < m; j++) {
+      const LaneIndex ix = mine.from(j);
+      if (!ix.keep) continue;
+      const double* r = vis5 + 5 * (t0 + j);
+      warp_scatter64(grid + (int64_t)ix.y0 * geo.pitch + ix.x0, geo.pitch,
+                     gcf + (int64_t)ix.phase * geo.S * geo.S, geo.S, r[3], r[4], lane);
+    }
   }
 }
 
 // vis_out = vis; in-bound: vis_out.re/im -= sum grid * gcf (degrid.cpp:78-98).
+// exps: largest exponent fields of the grid and the GCF; grid_df / gcf_df
+// their double-float splits (grid rows ext_x apart).
 __global__ void k_degrid_single64(int64_t n, const double* __restrict__ vis5,
                                   const double2* __restrict__ gcf,
-                                  const double2* __restrict__ grid, double* __restrict__ out5,
+                                  const double2* __restrict__ grid,
+                                  const float4* __restrict__ gcf_df,
+                                  const float4* __restrict__ grid_df,
+                                  const int* __restrict__ exps, double* __restrict__ out5,
                                   SingleGeo geo) {
   const int lane = threadIdx.x & 31;
+  const bool df = exps[0] != kExpNonFinite && exps[1] != kExpNonFinite;
+  const int kt = df_scale_exp(exps[0]) + df_scale_exp(exps[1]);
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
-  for (int64_t t = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5); t < n;
-       t += warps) {
-    const double* r = vis5 + 5 * t;
-    double* o = out5 + 5 * t;
-    const VisIndex ix = vis_index(r[0], r[1], geo.scale, geo.grid_size, geo.S, geo.margin,
-                                  geo.min_x, geo.min_y, geo.ext_x, geo.ext_y);
+  for (int64_t t0 = 32 * (blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5)); t0 < n;
+       t0 += 32 * warps) {
+    const int64_t t = t0 + lane;
+    const LaneIndex mine = single_index(vis5, t, n, geo);
+    const int m = (int)min((int64_t)32, n - t0);
+    float4 acc_df = make_float4(0.f, 0.f, 0.f, 0.f);
     double2 acc = make_double2(0.0, 0.0);
-    if (ix.keep) {
-      const double2* base =
-          grid + (int64_t)(ix.y0 - geo.min_y) * geo.pitch + (ix.x0 - geo.min_x);
-      acc = warp_gather64(base, geo.pitch, gcf + (int64_t)ix.phase * geo.S * geo.S, geo.S,
-                          false, lane);
+    for (int j = 0; j < m; j++) {
+      const LaneIndex ix = mine.from(j);
+      if (!ix.keep) continue;
+      const int64_t g0 = (int64_t)ix.phase * geo.S * geo.S;
+      if (df) {
+        const float4 a = warp_gather_df<false>(grid_df + (int64_t)ix.y0 * geo.ext_x + ix.x0,
+                                               geo.ext_x, gcf_df + g0, geo.S, lane);
+        if (lane == j) acc_df = a;
+      } else {
+        const double2 a = warp_gather64(grid + (int64_t)ix.y0 * geo.pitch + ix.x0, geo.pitch,
+                                        gcf + g0, geo.S, false, lane);
+        if (lane == j) acc = a;
+      }
     }
-    if (lane < 5) {
-      double val = r[lane];
-      if (lane == 3) val -= acc.x;
-      if (lane == 4) val -= acc.y;
-      o[lane] = val;
+    if (t < n) {
+      if (df) acc = df_to_double(acc_df, kt);
+      const double* r = vis5 + 5 * t;
+      double* o = out5 + 5 * t;
+      o[0] = r[0];
+      o[1] = r[1];
+      o[2] = r[2];
+      o[3] = r[3] - acc.x;  // acc is zero for an out-of-bound record
+      o[4] = r[4] - acc.y;
     }
   }
 }
 
 // ---------------------------------------------------------------- multi-plane (engine form)
+__device__ __forceinline__ LaneIndex plane_index(const PlanDev& P, int64_t t) {
+  LaneIndex li{0, 0, 0, 0, -1};
+  if (t < P.n_vis) {
+    const int32_t p = P.plane[t];
+    if (p >= 0) {
+      const double* r = P.uvw + t * P.uvw_stride;
+      const VisIndex ix = vis_index(r[0], r[1], P.scale, P.grid_size, P.supports[p], P.margin, 0,
+                                    0, P.ext_x, P.ext_y);
+      li = LaneIndex{ix.x0, ix.y0, ix.phase, ix.keep, p};
+    }
+  }
+  return li;
+}
+
 __global__ void k_grid_plain64(PlanDev P, const double2* __restrict__ vis,
                                const double2* __restrict__ gcf, double2* __restrict__ grid) {
   const int lane = threadIdx.x & 31;
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
-  for (int64_t t = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5); t < P.n_vis;
-       t += warps) {
-    const int32_t p = P.plane[t];
-    if (p < 0) continue;
-    const int32_t S = P.supports[p];
-    const double* r = P.uvw + t * P.uvw_stride;
-    const VisIndex ix =
-        vis_index(r[0], r[1], P.scale, P.grid_size, S, P.margin, 0, 0, P.ext_x, P.ext_y);
-    if (!ix.keep) continue;
-    const double2 v = vis[t];
-    warp_scatter64(grid + (int64_t)ix.y0 * P.pitch + ix.x0, P.pitch,
-                   gcf + P.gcf_offsets[p] + (int64_t)ix.phase * S * S, S, v.x, v.y, lane);
+  for (int64_t t0 = 32 * (blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5));
+       t0 < P.n_vis; t0 += 32 * warps) {
+    const LaneIndex mine = plane_index(P, t0 + lane);
+    const int m = (int)min((int64_t)32, P.n_vis - t0);
+    for (int j = 0; j < m; j++) {
+      const LaneIndex ix = mine.from(j);
+      if (!ix.keep) continue;
+      const int32_t S = P.supports[ix.plane];
+      const double2 v = vis[t0 + j];
+      warp_scatter64(grid + (int64_t)ix.y0 * P.pitch + ix.x0, P.pitch,
+                     gcf + P.gcf_offsets[ix.plane] + (int64_t)ix.phase * S * S, S, v.x, v.y,
+                     lane);
+    }
   }
 }
 
+// mode 0: pred = sum grid * conj(gcf); mode 1: pred = -sum grid * gcf.
+// grid_df rows are ext_x apart.
 __global__ void k_degrid_plain64(PlanDev P, const double2* __restrict__ gcf,
-                                 const double2* __restrict__ grid, double2* __restrict__ pred,
+                                 const double2* __restrict__ grid,
+                                 const float4* __restrict__ gcf_df,
+                                 const float4* __restrict__ grid_df,
+                                 const int* __restrict__ exps, double2* __restrict__ pred,
                                  int mode) {
   const int lane = threadIdx.x & 31;
+  const bool df = exps[0] != kExpNonFinite && exps[1] != kExpNonFinite;
+  const int kt = df_scale_exp(exps[0]) + df_scale_exp(exps[1]);
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
-  for (int64_t t = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5); t < P.n_vis;
-       t += warps) {
-    const int32_t p = P.plane[t];
+  for (int64_t t0 = 32 * (blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5));
+       t0 < P.n_vis; t0 += 32 * warps) {
+    const int64_t t = t0 + lane;
+    const LaneIndex mine = plane_index(P, t);
+    const int m = (int)min((int64_t)32, P.n_vis - t0);
+    float4 acc_df = make_float4(0.f, 0.f, 0.f, 0.f);
     double2 acc = make_double2(0.0, 0.0);
-    if (p >= 0) {
-      const int32_t S = P.supports[p];
-      const double* r = P.uvw + t * P.uvw_stride;
-      const VisIndex ix =
-          vis_index(r[0], r[1], P.scale, P.grid_size, S, P.margin, 0, 0, P.ext_x, P.ext_y);
-      if (ix.keep) {
-        acc = warp_gather64(grid + (int64_t)ix.y0 * P.pitch + ix.x0, P.pitch,
-                            gcf + P.gcf_offsets[p] + (int64_t)ix.phase * S * S, S, mode == 0,
-                            lane);
-        if (mode == 1) {
-          acc.x = -acc.x;
-          acc.y = -acc.y;
-        }
+    for (int j = 0; j < m; j++) {
+      const LaneIndex ix = mine.from(j);
+      if (!ix.keep) continue;
+      const int32_t S = P.supports[ix.plane];
+      const int64_t g0 = P.gcf_offsets[ix.plane] + (int64_t)ix.phase * S * S;
+      if (df) {
+        const float4* base = grid_df + (int64_t)ix.y0 * P.ext_x + ix.x0;
+        const float4 a = mode == 0 ? warp_gather_df<true>(base, P.ext_x, gcf_df + g0, S, lane)
+                                   : warp_gather_df<false>(base, P.ext_x, gcf_df + g0, S, lane);
+        if (lane == j) acc_df = a;
+      } else {
+        const double2 a = warp_gather64(grid + (int64_t)ix.y0 * P.pitch + ix.x0, P.pitch,
+                                        gcf + g0, S, mode == 0, lane);
+        if (lane == j) acc = a;
       }
     }
-    if (lane == 0) pred[t] = acc;
+    if (t < P.n_vis) {
+      if (df) acc = df_to_double(acc_df, kt);
+      if (mode == 1) {
+        acc.x = -acc.x;
+        acc.y = -acc.y;
+      }
+      pred[t] = acc;
+    }
   }
 }
 
 static int plain_grid_dims(int64_t n, int* blocks) {
-  const int64_t warps_needed = n;
+  const int64_t warps_needed = (n + 31) / 32;
   int64_t b = (warps_needed + 7) / 8;
-  const int64_t cap = (int64_t)sm_count() * 16;
+  const int64_t cap = (int64_t)sm_count() * 8;
   if (b > cap) b = cap;
   if (b < 1) b = 1;
   *blocks = (int)b;
   return 256;
+}
+
+// Exponents and double-float splits of a grid region (ext_y rows of ext_x
+// complex elements, `pitch` apart) and of n_gcf complex GCF elements.
+static int df_prepare(const double* grid, int32_t ext_x, int32_t ext_y, int64_t pitch,
+                      const double* gcf, int64_t n_gcf, float4* grid_df, float4* gcf_df,
+                      int* exps, cudaStream_t s) {
+  GB_CUDA_TRY(cudaMemsetAsync(exps, 0, 2 * sizeof(int), s));
+  const int64_t row = 2 * (int64_t)ext_x;
+  const dim3 gg((unsigned)std::clamp<int64_t>((row + 255) / 256, 1, 64),
+                (unsigned)std::clamp<int64_t>(ext_y, 1, 4096));
+  const dim3 gc((unsigned)std::clamp<int64_t>((2 * n_gcf + 255) / 256, 1, (int64_t)sm_count() * 4),
+                1);
+  k_max_exponent<<<gg, 256, 0, s>>>(grid, ext_y, row, 2 * pitch, exps);
+  k_max_exponent<<<gc, 256, 0, s>>>(gcf, 1, 2 * n_gcf, 2 * n_gcf, exps + 1);
+  k_df_split<<<gg, 256, 0, s>>>(grid, ext_y, row, 2 * pitch, exps, 0, (float2*)grid_df);
+  k_df_split<<<gc, 256, 0, s>>>(gcf, 1, 2 * n_gcf, 2 * n_gcf, exps, 1, (float2*)gcf_df);
+  GB_CUDA_TRY(cudaGetLastError());
+  return GB_OK;
+}
+
+int df_reserve(DfScratch& d, int64_t grid_elems, int64_t gcf_elems) {
+  int rc;
+  if (!d.exps && (rc = dev_alloc((void**)&d.exps, 2 * sizeof(int), "FP64 degrid scratch")))
+    return rc;
+  if ((size_t)grid_elems > d.grid_cap) {
+    cudaFree(d.grid);
+    d.grid = nullptr;
+    d.grid_cap = 0;
+    if ((rc = dev_alloc((void**)&d.grid, sizeof(float4) * grid_elems, "FP64 degrid scratch")))
+      return rc;
+    d.grid_cap = grid_elems;
+  }
+  if ((size_t)gcf_elems > d.gcf_cap) {
+    cudaFree(d.gcf);
+    d.gcf = nullptr;
+    d.gcf_cap = 0;
+    if ((rc = dev_alloc((void**)&d.gcf, sizeof(float4) * gcf_elems, "FP64 degrid scratch")))
+      return rc;
+    d.gcf_cap = gcf_elems;
+  }
+  return GB_OK;
+}
+
+void DfScratch::release() {
+  cudaFree(grid);
+  cudaFree(gcf);
+  cudaFree(exps);
+  grid = gcf = nullptr;
+  exps = nullptr;
+  grid_cap = gcf_cap = 0;
 }
 
 int launch_grid_plain64(const gb_plan* plan, const double* vis, const double* gcf, double* grid,
@@ -196,11 +467,18 @@ int launch_grid_plain64(const gb_plan* plan, const double* vis, const double* gc
 }
 
 int launch_degrid_plain64(const gb_plan* plan, const double* gcf, const double* grid,
-                          double* pred, int mode, cudaStream_t s) {
+                          double* pred, int mode, DfScratch& scratch, cudaStream_t s) {
+  const PlanDev& D = plan->dev;
+  int rc;
+  if ((rc = df_reserve(scratch, (int64_t)D.ext_x * D.ext_y, plan->gcf_len)) ||
+      (rc = df_prepare(grid, D.ext_x, D.ext_y, D.pitch, gcf, plan->gcf_len, scratch.grid,
+                       scratch.gcf, scratch.exps, s)))
+    return rc;
   int blocks;
-  const int threads = plain_grid_dims(plan->dev.n_vis, &blocks);
-  k_degrid_plain64<<<blocks, threads, 0, s>>>(plan->dev, (const double2*)gcf,
-                                              (const double2*)grid, (double2*)pred, mode);
+  const int threads = plain_grid_dims(D.n_vis, &blocks);
+  k_degrid_plain64<<<blocks, threads, 0, s>>>(D, (const double2*)gcf, (const double2*)grid,
+                                              scratch.gcf, scratch.grid, scratch.exps,
+                                              (double2*)pred, mode);
   GB_CUDA_TRY(cudaGetLastError());
   return GB_OK;
 }
@@ -325,10 +603,16 @@ static int compat_degrid(const char* who, int size_err, double scale, int32_t gr
   void *d_vis, *d_gcf, *d_grid, *d_out;
   const size_t gcf_bytes = (size_t)GB_PHASES * S * S * 16;
   const size_t grid_bytes = (size_t)W * H * 16;
+  // slots 4 / 5: the grid and the GCF as double-float pairs (same sizes), the
+  // two exponent words after the GCF's
+  void *d_grid_df, *d_gcf_df;
   if ((rc = stage_buffer(0, (size_t)n * 40, &d_vis)) || (rc = stage_buffer(1, gcf_bytes, &d_gcf)) ||
-      (rc = stage_buffer(2, grid_bytes, &d_grid)) || (rc = stage_buffer(3, (size_t)n * 40, &d_out)))
+      (rc = stage_buffer(2, grid_bytes, &d_grid)) || (rc = stage_buffer(3, (size_t)n * 40, &d_out)) ||
+      (rc = stage_buffer(4, grid_bytes, &d_grid_df)) ||
+      (rc = stage_buffer(5, gcf_bytes + 16, &d_gcf_df)))
     return rc;
   if (n == 0) return GB_OK;
+  int* d_exps = (int*)((char*)d_gcf_df + gcf_bytes);
   GB_CUDA_TRY(cudaMemcpyAsync(d_vis, (const double*)vis->host + 5 * first, (size_t)n * 40,
                               cudaMemcpyHostToDevice, s));
   GB_CUDA_TRY(cudaMemcpyAsync(d_gcf, gcf->host, gcf_bytes, cudaMemcpyHostToDevice, s));
@@ -337,8 +621,13 @@ static int compat_degrid(const char* who, int size_err, double scale, int32_t gr
   SingleGeo geo{scale, grid_size, margin, S, uvg->min[1], uvg->min[2], W, H, (int64_t)W};
   int blocks;
   const int threads = plain_grid_dims(n, &blocks);
-  k_degrid_single64<<<blocks, threads, 0, s>>>(n, (const double*)d_vis, (const double2*)d_gcf,
-                                               (const double2*)d_grid, (double*)d_out, geo);
+  if ((rc = df_prepare((const double*)d_grid, W, H, W, (const double*)d_gcf,
+                       (int64_t)GB_PHASES * S * S, (float4*)d_grid_df, (float4*)d_gcf_df, d_exps,
+                       s)))
+    return rc;
+  k_degrid_single64<<<blocks, threads, 0, s>>>(
+      n, (const double*)d_vis, (const double2*)d_gcf, (const double2*)d_grid,
+      (const float4*)d_gcf_df, (const float4*)d_grid_df, d_exps, (double*)d_out, geo);
   GB_CUDA_TRY(cudaGetLastError());
   GB_CUDA_TRY(cudaMemcpyAsync(vis_out->host, d_out, (size_t)n * 40, cudaMemcpyDeviceToHost, s));
   GB_CUDA_TRY(cudaStreamSynchronize(s));

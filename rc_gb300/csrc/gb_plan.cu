@@ -167,6 +167,7 @@ static void free_plan(gb_plan* p) {
   cudaFree(p->d_items);
   cudaFree(p->d_bundles);
   cudaFree(p->d_queue);
+  p->df.release();
   delete p;
 }
 
@@ -628,5 +629,5 @@ extern "C" int gb_degrid_f64(gb_plan* P, const double* d_gcf, const double* d_gr
     return GB_ERR_ARG;
   }
   if (P->dev.n_vis == 0) return GB_OK;
-  return launch_degrid_plain64(P, d_gcf, d_grid, d_pred, mode, (cudaStream_t)stream);
+  return launch_degrid_plain64(P, d_gcf, d_grid, d_pred, mode, P->df, (cudaStream_t)stream);
 }

@@ -121,6 +121,19 @@ struct PlaneInfo {
   int64_t gcf_off;
 };
 
+// Scratch of the FP64 degridder (gb_plain.cu): the grid region and the GCFs
+// split into double-float pairs, and the two arrays' largest exponent fields.
+// Grown on demand; owned by a plan or a batch.
+struct DfScratch {
+  float4* grid = nullptr;  // ext_x * ext_y complex elements
+  size_t grid_cap = 0;
+  float4* gcf = nullptr;
+  size_t gcf_cap = 0;
+  int* exps = nullptr;  // [0] grid, [1] GCF
+  void release();
+};
+int df_reserve(DfScratch& d, int64_t grid_elems, int64_t gcf_elems);
+
 }  // namespace gb
 
 struct gb_plan {
@@ -167,6 +180,7 @@ struct gb_plan {
   bool tma_ok = false;
   CUtensorMap tma_maps[gb::kMaxClasses];
   int last_stage = 0;  // GB_STAGE_* form of the last degridding launch
+  gb::DfScratch df;    // FP64 degridding scratch, allocated by its first call
 };
 
 namespace gb {
@@ -178,7 +192,7 @@ void make_bundles(const std::vector<HostItem>& items, const ClassInfo* cls, int 
 int launch_grid_plain64(const gb_plan* plan, const double* vis, const double* gcf, double* grid,
                         cudaStream_t s);
 int launch_degrid_plain64(const gb_plan* plan, const double* gcf, const double* grid,
-                          double* pred, int mode, cudaStream_t s);
+                          double* pred, int mode, DfScratch& scratch, cudaStream_t s);
 int launch_grid_tiled(gb_plan* plan, const float* vis, const float* gcf, float* grid,
                       cudaStream_t s);
 int launch_degrid_tiled(gb_plan* plan, const float* gcf, const float* grid, float* pred,
