@@ -221,7 +221,12 @@ int gb_degrid_backward(gb_plan *plan, const float *d_gcf, const float *d_pred_gr
                        float *d_grid_grad, void *stream);
 
 /* Plain FP64 path (complex128): no tiling, no sorting; one warp per
- * visibility, FP64 atomics into the grid.  Same operators as above. */
+ * visibility, FP64 atomics into the grid.  Same operators as above.
+ * Degridding computes in double-float (every double held as two floats, to
+ * 2^-48; sums to about 2^-48 of the running sum) and takes the native FP64
+ * loop when the grid or the GCF holds an Inf, a NaN or a subnormal.  Its
+ * first call on a plan allocates the plan's scratch (16 bytes per grid cell
+ * of ext_x x ext_y and per GCF element): make it before any stream capture. */
 int gb_grid_f64(gb_plan *plan, const double *d_vis, const double *d_gcf, double *d_grid,
                 void *stream);
 int gb_degrid_f64(gb_plan *plan, const double *d_gcf, const double *d_grid,
@@ -322,7 +327,9 @@ int gb_batch_grid_f32(gb_batch *batch, const float *const *d_vis, const float *d
                       float *const *d_grids, void *stream);
 int gb_batch_degrid_f32(gb_batch *batch, const float *d_gcf, const float *const *d_grids,
                         float *const *d_preds, int32_t mode, void *stream);
-/* The plain FP64 path over the members (one launch per member, complex128). */
+/* The plain FP64 path over the members (one launch per member, complex128).
+ * Degridding as gb_degrid_f64, with one scratch for the batch, grown to the
+ * largest member on the first call. */
 int gb_batch_grid_f64(gb_batch *batch, const double *const *d_vis, const double *d_gcf,
                       double *const *d_grids, void *stream);
 int gb_batch_degrid_f64(gb_batch *batch, const double *d_gcf, const double *const *d_grids,
