@@ -3,7 +3,9 @@
 //
 // "Plain" = no sorting, no tiling, no shared memory: one warp per
 // visibility, lanes over the S*S taps, FP64 atomics into the grid (gridding)
-// or a warp-shuffle reduction (degridding).  It is the FP64 GPU comparison
+// or a warp-shuffle reduction (degridding, computed in double-float; see the
+// section below).  Each lane computes the FP64 index math of one of 32
+// visibilities and the warp takes them in turn.  It is the FP64 GPU comparison
 // path of the engine and the implementation behind kern_scatter_gpu1 /
 // kern_degrid_gpu1 / nvGridder / kern_scatter / kern_degrid, whose semantics
 // are the reference's (MS6/kernel/cpu/gridding/scatter.cpp:56-111,
