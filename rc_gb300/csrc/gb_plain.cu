@@ -26,11 +26,12 @@ namespace gb {
 // 32 m, (i, j) = (k mod S, k div S), advanced incrementally.
 struct TapWalk {
   int i, j, di, dj, S;
-  __device__ __forceinline__ TapWalk(int S_, int lane) : S(S_) {
+  // lane: the lane's index among the L lanes that share the footprint
+  __device__ __forceinline__ TapWalk(int S_, int lane, int L = 32) : S(S_) {
     j = lane / S_;
     i = lane - j * S_;
-    dj = 32 / S_;
-    di = 32 - dj * S_;
+    dj = L / S_;
+    di = L - dj * S_;
   }
   __device__ __forceinline__ void next() {
     i += di;
@@ -188,19 +189,22 @@ __device__ __forceinline__ void df_cmac(const float4 a, float4 b, float4& acc) {
   two_sum_acc(acc.y, acc.w, p4);
 }
 
-template <bool CONJ>
+// The footprint's double-float sum over a group of L lanes (an aligned part
+// of the warp, `mask` its lanes; lane = the lane's index in the group).
+template <bool CONJ, int L = 32>
 __device__ __forceinline__ float4 warp_gather_df(const float4* __restrict__ base, int64_t pitch,
-                                                 const float4* __restrict__ g, int S, int lane) {
+                                                 const float4* __restrict__ g, int S, int lane,
+                                                 unsigned mask = 0xffffffffu) {
   float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-  TapWalk w(S, lane);
+  TapWalk w(S, lane, L);
   for (; w.j < S; w.next())
     df_cmac<CONJ>(base[(int64_t)w.j * pitch + w.i], __ldg(g + w.j * S + w.i), acc);
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    const float sr = __shfl_xor_sync(0xffffffffu, acc.x, o);
-    const float si = __shfl_xor_sync(0xffffffffu, acc.y, o);
-    acc.z = __fadd_rn(acc.z, __shfl_xor_sync(0xffffffffu, acc.z, o));
-    acc.w = __fadd_rn(acc.w, __shfl_xor_sync(0xffffffffu, acc.w, o));
+  for (int o = L / 2; o > 0; o >>= 1) {
+    const float sr = __shfl_xor_sync(mask, acc.x, o);
+    const float si = __shfl_xor_sync(mask, acc.y, o);
+    acc.z = __fadd_rn(acc.z, __shfl_xor_sync(mask, acc.z, o));
+    acc.w = __fadd_rn(acc.w, __shfl_xor_sync(mask, acc.w, o));
     two_sum_acc(acc.x, acc.z, sr);
     two_sum_acc(acc.y, acc.w, si);
   }
@@ -289,7 +293,28 @@ __global__ void k_degrid_single64(int64_t n, const double* __restrict__ vis5,
     const int m = (int)min((int64_t)32, n - t0);
     float4 acc_df = make_float4(0.f, 0.f, 0.f, 0.f);
     double2 acc = make_double2(0.0, 0.0);
-    for (int j = 0; j < m; j++) {
+    if (df && geo.S <= 8) {
+      // small footprints: 8 lanes per visibility, four visibilities at a time
+      const int grp = lane >> 3, gl = lane & 7;
+      const unsigned gmask = 0xFFu << (8 * grp);
+      for (int j0 = 0; j0 < m; j0 += 4) {
+        const int jv = j0 + grp;
+        const LaneIndex ix = mine.from(jv < m ? jv : m - 1);
+        float4 a = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (jv < m && ix.keep)  // uniform within the group
+          a = warp_gather_df<false, 8>(grid_df + (int64_t)ix.y0 * geo.ext_x + ix.x0, geo.ext_x,
+                                       gcf_df + (int64_t)ix.phase * geo.S * geo.S, geo.S, gl,
+                                       gmask);
+        // lane j0 + q takes the sum of group q
+        const int src = ((lane - j0) & 3) * 8;
+        a.x = __shfl_sync(0xffffffffu, a.x, src);
+        a.y = __shfl_sync(0xffffffffu, a.y, src);
+        a.z = __shfl_sync(0xffffffffu, a.z, src);
+        a.w = __shfl_sync(0xffffffffu, a.w, src);
+        if (lane >= j0 && lane < j0 + 4) acc_df = a;
+      }
+    }
+    for (int j = 0; j < m && !(df && geo.S <= 8); j++) {
       const LaneIndex ix = mine.from(j);
       if (!ix.keep) continue;
       const int64_t g0 = (int64_t)ix.phase * geo.S * geo.S;
@@ -407,6 +432,15 @@ static int plain_grid_dims(int64_t n, int* blocks) {
   return 256;
 }
 
+// a += b over n complex128 elements.
+__global__ void k_add_c128(double2* __restrict__ a, const double2* __restrict__ b, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const double2 x = a[i], y = b[i];
+    a[i] = make_double2(x.x + y.x, x.y + y.y);
+  }
+}
+
 // Exponents and double-float splits of a grid region (ext_y rows of ext_x
 // complex elements, `pitch` apart) and of n_gcf complex GCF elements.
 static int df_prepare(const double* grid, int32_t ext_x, int32_t ext_y, int64_t pitch,
@@ -485,6 +519,21 @@ int launch_degrid_plain64(const gb_plan* plan, const double* gcf, const double* 
   return GB_OK;
 }
 
+// A CUDA call of an ABI entry point that has work queued on two streams: on an
+// error both streams are drained before returning, so that nothing still
+// reads or writes the caller's buffers afterwards.
+#define GB_TRY_DRAIN(expr, s_a, s_b)                                              \
+  do {                                                                            \
+    const cudaError_t _e = (expr);                                                \
+    if (_e != cudaSuccess) {                                                      \
+      gb_set_error(GB_ERR_CUDA, "%s:%d %s: %s", __FILE__, __LINE__, #expr,        \
+                   cudaGetErrorString(_e));                                       \
+      cudaStreamSynchronize(s_a);                                                 \
+      cudaStreamSynchronize(s_b);                                                 \
+      return GB_ERR_CUDA;                                                         \
+    }                                                                             \
+  } while (0)
+
 // ---------------------------------------------------------------- buffer_t validation
 // GCF size as the reference dispatchers read it (gcf_common.h:8-14).
 static int32_t check_size(const buffer_t* gcf) {
@@ -550,26 +599,39 @@ static int compat_scatter(const char* who, int size_err, double scale, int32_t g
   const int64_t n = vis->extent[1];
   const int32_t W = uvg->extent[1], H = uvg->extent[2];
   const int64_t row = grid_row_doubles(uvg);
-  cudaStream_t s;
-  if ((rc = stage_stream(&s))) return rc;
-  void *d_vis, *d_gcf, *d_grid;
+  if (n == 0) return GB_OK;  // the grid is unchanged
+  cudaStream_t s, s2;
+  cudaEvent_t ev;
+  if ((rc = stage_stream(&s)) || (rc = stage_aux(&s2, &ev))) return rc;
+  void *d_vis, *d_gcf, *d_grid, *d_acc;
   const size_t gcf_bytes = (size_t)GB_PHASES * S * S * 16;
   const size_t grid_bytes = (size_t)W * H * 16;
   if ((rc = stage_buffer(0, (size_t)n * 40, &d_vis)) || (rc = stage_buffer(1, gcf_bytes, &d_gcf)) ||
-      (rc = stage_buffer(2, grid_bytes, &d_grid)))
+      (rc = stage_buffer(2, grid_bytes, &d_grid)) || (rc = stage_buffer(4, grid_bytes, &d_acc)))
     return rc;
-  if (n > 0) GB_CUDA_TRY(cudaMemcpyAsync(d_vis, vis->host, (size_t)n * 40, cudaMemcpyHostToDevice, s));
+  // Visibilities and GCF first.  The kernel then grids into a zeroed buffer on
+  // the second stream while the caller's grid comes up on the first; the two
+  // are added before the grid goes back.
+  GB_CUDA_TRY(cudaMemcpyAsync(d_vis, vis->host, (size_t)n * 40, cudaMemcpyHostToDevice, s));
   GB_CUDA_TRY(cudaMemcpyAsync(d_gcf, gcf->host, gcf_bytes, cudaMemcpyHostToDevice, s));
-  GB_CUDA_TRY(cudaMemcpy2DAsync(d_grid, (size_t)W * 16, uvg->host, (size_t)row * 8, (size_t)W * 16,
-                                H, cudaMemcpyHostToDevice, s));
-  if (n > 0) {
-    SingleGeo geo{scale, grid_size, margin, S, uvg->min[1], uvg->min[2], W, H, (int64_t)W};
-    int blocks;
-    const int threads = plain_grid_dims(n, &blocks);
-    k_scatter_single64<<<blocks, threads, 0, s>>>(n, (const double*)d_vis, (const double2*)d_gcf,
-                                                  (double2*)d_grid, geo);
-    GB_CUDA_TRY(cudaGetLastError());
-  }
+  GB_CUDA_TRY(cudaMemsetAsync(d_acc, 0, grid_bytes, s));
+  GB_CUDA_TRY(cudaEventRecord(ev, s));
+  GB_CUDA_TRY(cudaStreamWaitEvent(s2, ev, 0));
+  SingleGeo geo{scale, grid_size, margin, S, uvg->min[1], uvg->min[2], W, H, (int64_t)W};
+  int blocks;
+  const int threads = plain_grid_dims(n, &blocks);
+  k_scatter_single64<<<blocks, threads, 0, s2>>>(n, (const double*)d_vis, (const double2*)d_gcf,
+                                                 (double2*)d_acc, geo);
+  GB_TRY_DRAIN(cudaGetLastError(), s, s2);
+  GB_TRY_DRAIN(cudaEventRecord(ev, s2), s, s2);
+  GB_TRY_DRAIN(cudaMemcpy2DAsync(d_grid, (size_t)W * 16, uvg->host, (size_t)row * 8,
+                                 (size_t)W * 16, H, cudaMemcpyHostToDevice, s),
+               s, s2);
+  GB_TRY_DRAIN(cudaStreamWaitEvent(s, ev, 0), s, s2);
+  const int64_t cells = (int64_t)W * H;
+  k_add_c128<<<(unsigned)std::clamp<int64_t>((cells + 255) / 256, 1, (int64_t)sm_count() * 8), 256,
+               0, s>>>((double2*)d_grid, (const double2*)d_acc, cells);
+  GB_CUDA_TRY(cudaGetLastError());
   GB_CUDA_TRY(cudaMemcpy2DAsync(uvg->host, (size_t)row * 8, d_grid, (size_t)W * 16, (size_t)W * 16,
                                 H, cudaMemcpyDeviceToHost, s));
   GB_CUDA_TRY(cudaStreamSynchronize(s));
@@ -621,17 +683,31 @@ static int compat_degrid(const char* who, int size_err, double scale, int32_t gr
   GB_CUDA_TRY(cudaMemcpy2DAsync(d_grid, (size_t)W * 16, uvg->host, (size_t)row * 8, (size_t)W * 16,
                                 H, cudaMemcpyHostToDevice, s));
   SingleGeo geo{scale, grid_size, margin, S, uvg->min[1], uvg->min[2], W, H, (int64_t)W};
-  int blocks;
-  const int threads = plain_grid_dims(n, &blocks);
   if ((rc = df_prepare((const double*)d_grid, W, H, W, (const double*)d_gcf,
                        (int64_t)GB_PHASES * S * S, (float4*)d_grid_df, (float4*)d_gcf_df, d_exps,
                        s)))
     return rc;
-  k_degrid_single64<<<blocks, threads, 0, s>>>(
-      n, (const double*)d_vis, (const double2*)d_gcf, (const double2*)d_grid,
-      (const float4*)d_gcf_df, (const float4*)d_grid_df, d_exps, (double*)d_out, geo);
-  GB_CUDA_TRY(cudaGetLastError());
-  GB_CUDA_TRY(cudaMemcpyAsync(vis_out->host, d_out, (size_t)n * 40, cudaMemcpyDeviceToHost, s));
+  // in chunks of visibilities: a chunk's results go down on the second stream
+  // while the next chunk is degridded
+  cudaStream_t s2;
+  cudaEvent_t ev;
+  if ((rc = stage_aux(&s2, &ev))) return rc;
+  const int chunks = n >= (1 << 18) ? 4 : 1;
+  for (int c = 0; c < chunks; c++) {
+    const int64_t c0 = n * c / chunks, c1 = n * (c + 1) / chunks;
+    int blocks;
+    const int threads = plain_grid_dims(c1 - c0, &blocks);
+    k_degrid_single64<<<blocks, threads, 0, s>>>(
+        c1 - c0, (const double*)d_vis + 5 * c0, (const double2*)d_gcf, (const double2*)d_grid,
+        (const float4*)d_gcf_df, (const float4*)d_grid_df, d_exps, (double*)d_out + 5 * c0, geo);
+    GB_TRY_DRAIN(cudaGetLastError(), s, s2);
+    GB_TRY_DRAIN(cudaEventRecord(ev, s), s, s2);
+    GB_TRY_DRAIN(cudaStreamWaitEvent(s2, ev, 0), s, s2);
+    GB_TRY_DRAIN(cudaMemcpyAsync((double*)vis_out->host + 5 * c0, (const double*)d_out + 5 * c0,
+                                 (size_t)(c1 - c0) * 40, cudaMemcpyDeviceToHost, s2),
+                 s, s2);
+  }
+  GB_TRY_DRAIN(cudaStreamSynchronize(s2), s, s2);
   GB_CUDA_TRY(cudaStreamSynchronize(s));
   return GB_OK;
 }

@@ -34,14 +34,23 @@ namespace gb {
 // -threaded program), so every thread gets its own stream and buffers.
 struct Staging {
   cudaStream_t stream = nullptr;
+  cudaStream_t stream2 = nullptr;  // overlaps copies with kernels inside one call
+  cudaEvent_t event = nullptr;
   int device = -1;
   void* buf[kStageSlots] = {};
   size_t cap[kStageSlots] = {};
+  void release_aux() {
+    if (event) cudaEventDestroy(event);
+    if (stream2) cudaStreamDestroy(stream2);
+    event = nullptr;
+    stream2 = nullptr;
+  }
   ~Staging() {
     // Released at thread exit; errors are ignored because the context may
     // already be gone at process teardown.
     for (int i = 0; i < kStageSlots; i++)
       if (buf[i]) cudaFree(buf[i]);
+    release_aux();
     if (stream) cudaStreamDestroy(stream);
   }
 };
@@ -58,6 +67,7 @@ int stage_stream(cudaStream_t* out) {
       t_stage.buf[i] = nullptr;
       t_stage.cap[i] = 0;
     }
+    t_stage.release_aux();
     cudaStreamDestroy(t_stage.stream);
     t_stage.stream = nullptr;
   }
@@ -66,6 +76,18 @@ int stage_stream(cudaStream_t* out) {
     t_stage.device = dev;
   }
   *out = t_stage.stream;
+  return GB_OK;
+}
+
+int stage_aux(cudaStream_t* s2, cudaEvent_t* ev) {
+  cudaStream_t s;
+  int rc;
+  if ((rc = stage_stream(&s))) return rc;  // also drops the aux objects of another device
+  if (!t_stage.stream2)
+    GB_CUDA_TRY(cudaStreamCreateWithFlags(&t_stage.stream2, cudaStreamNonBlocking));
+  if (!t_stage.event) GB_CUDA_TRY(cudaEventCreateWithFlags(&t_stage.event, cudaEventDisableTiming));
+  *s2 = t_stage.stream2;
+  *ev = t_stage.event;
   return GB_OK;
 }
 

@@ -12,6 +12,9 @@ constexpr int kStageSlots = 6;
 // reference-ABI entry points.
 int stage_stream(cudaStream_t* out);
 int stage_buffer(int slot, size_t bytes, void** out);
+// A second stream and an event of the same thread, for overlapping a call's
+// copies with its kernels.
+int stage_aux(cudaStream_t* s2, cudaEvent_t* ev);
 
 int sm_count();
 
