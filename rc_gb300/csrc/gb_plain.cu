@@ -660,6 +660,7 @@ static int compat_degrid(const char* who, int size_err, double scale, int32_t gr
     gb_set_error(GB_ERR_ARG, "%s: vis does not cover the vis_out region", who);
     return GB_ERR_ARG;
   }
+  if (n == 0) return GB_OK;  // nothing to write
   const int32_t W = uvg->extent[1], H = uvg->extent[2];
   const int64_t row = grid_row_doubles(uvg);
   cudaStream_t s;
@@ -675,7 +676,6 @@ static int compat_degrid(const char* who, int size_err, double scale, int32_t gr
       (rc = stage_buffer(4, grid_bytes, &d_grid_df)) ||
       (rc = stage_buffer(5, gcf_bytes + 16, &d_gcf_df)))
     return rc;
-  if (n == 0) return GB_OK;
   int* d_exps = (int*)((char*)d_gcf_df + gcf_bytes);
   GB_CUDA_TRY(cudaMemcpyAsync(d_vis, (const double*)vis->host + 5 * first, (size_t)n * 40,
                               cudaMemcpyHostToDevice, s));

@@ -90,3 +90,25 @@ def test_legacy_codes_are_the_reference_values():
     hdr = open(HEADER).read()
     for code in ["-444", "-555", "-222", "-333"]:
         assert f"({code})" in hdr
+
+
+def test_empty_calls_need_no_gpu():
+    """Zero visibilities: the reference-ABI gridders and degridders check their
+    buffers and return 0 without GPU work; the grid is left as it was."""
+    import numpy as np
+
+    from rc_gb300 import compat
+
+    lib.load()
+    vis5 = np.zeros((0, 5))
+    gcf = np.ones((64, 8, 8), np.complex128)
+    grid = np.full((16, 16), 1 + 2j)
+    for name in ("kern_scatter_gpu1", "kern_scatter", "nvGridder"):
+        assert compat.call_scatter(name, 1.0, 16, 8, vis5, gcf, grid) == 0
+    assert (grid == 1 + 2j).all()
+    out = np.zeros((0, 5))
+    for name in ("kern_degrid_gpu1", "kern_degrid"):
+        assert compat.call_degrid(name, 1.0, 16, 8, gcf, grid, vis5, out) == 0
+    # the size codes still come first
+    assert compat.call_scatter("kern_scatter_gpu1", 1.0, 16, 8, vis5,
+                               np.ones((64, 12, 12), np.complex128), grid) == -222
