@@ -1,0 +1,346 @@
+// rc_kernels.hpp -- C++17 host layer over librc_gb300's reference ABI for the
+// gridding path, mirroring the MS6 Haskell kernel bindings that drive it
+// (MS6/programs/Kernel/{Config,Data,Binning,IO,Gridder,Degrid,FFT}.hs): the
+// same kernel names and argument meanings, the same buffer layouts passed to
+// the same C symbols, and an exception where the Haskell marshaller gives up
+// with `error "Could not call Halide kernel!"` (MS6/dna/flow/Flow/Halide/
+// Marshal.hs:119-124).  Header only; link librc_gb300.so.
+//
+// The Haskell layer runs these kernels under the Flow scheduler, one call per
+// region (a u/v tile, a w-bin); here the caller makes those calls, e.g. the
+// gridding strategy of MS6/programs/gridding.hs:
+//
+//   for each (u, v) tile:   bins = binSizer(gp, vis, u, v)
+//                           vb   = binner(gp, vis, u, v, bins)
+//                           tile = gridInit(gcfp, u, v)
+//                           for each bin b: gridKernel(kt, gp, gcfp, vb[b], gcfKernel(gcfp, b.bin), tile)
+//                           gridDetiling(tile, full)            (full = gridInitDetile(...))
+//   image = ifftKern(gp, full)
+#pragma once
+
+#include <stdint.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "rc_gb300.h"
+
+namespace rc {
+
+// A non-zero status from a kernel call (the status and gb_last_error()).
+struct KernelError : std::runtime_error {
+  int code;
+  KernelError(const std::string& what, int c) : std::runtime_error(what), code(c) {}
+};
+
+inline void check(int status, const char* kernel) {
+  if (status != 0)
+    throw KernelError(std::string("Could not call kernel ") + kernel + " (" +
+                          std::to_string(status) + "): " + gb_last_error(),
+                      status);
+}
+
+// ------------------------------------------------------------ Kernel.Config
+// MS6/programs/Kernel/Config.hs:84-95
+struct GridPar {
+  int width = 0, height = 0, pitch = 0;
+  double theta = 0;  // field of view in radians
+  int tiles = 1, facets = 1, bins = 1;
+};
+
+// Config.hs:106-122
+struct GCFFile {
+  std::string file;
+  int size = 0;
+  double w = 0;
+};
+struct GCFPar {
+  std::vector<GCFFile> files;
+  int over = 8;
+};
+
+// Config.hs:52-66: the symbol each kernel type binds (Gridder.hs:58-63, Degrid.hs:148-152)
+enum class GridKernelType { CPU, GPU, NV };
+enum class DegridKernelType { CPU, GPU };
+
+// Config.hs:124-125
+inline int gcfMaxSize(const GCFPar& p) {
+  int m = 0;
+  for (const GCFFile& f : p.files) m = std::max(m, f.size);
+  return m;
+}
+
+// Config.hs:128-132: the file with the largest w <= max(|w0|, |w1|) (the
+// last of equal ones); none is an error there too (maximumBy of an empty list).
+inline const GCFFile& gcfGet(const GCFPar& p, double w0, double w1) {
+  std::vector<double> ws;
+  for (const GCFFile& f : p.files) ws.push_back(f.w);
+  int32_t index = -1, conj = 0;
+  check(gb_gcf_select((int32_t)ws.size(), ws.data(), w0, w1, &index, &conj), "gcfGet");
+  return p.files[index];
+}
+
+// Config.hs:199-212
+inline int gridImageWidth(const GridPar& gp) { return gp.width * gp.facets; }
+inline int gridImageHeight(const GridPar& gp) { return gp.height * gp.facets; }
+inline double gridScale(const GridPar& gp) { return gp.theta / (double)gp.facets; }
+inline double gridXY2UV(const GridPar& gp, int z) {
+  return (double)(z - gp.height / 2) / gridScale(gp);
+}
+
+// ------------------------------------------------------------ Kernel.Data
+// A region of a range domain: pixels [low, high).
+struct Range {
+  int low = 0, high = 0;
+  int size() const { return high - low; }
+};
+
+// A region of a bin domain (Flow.Domain RegionBinDesc): w in [low, high),
+// `count` records.
+struct WBin {
+  double low = 0, high = 0;
+  int64_t count = 0;
+};
+
+// Visibilities: 5-double records u, v, w, re, im (Data.hs:115-123).
+struct Vis {
+  std::vector<double> rec;
+  int64_t size() const { return (int64_t)rec.size() / 5; }
+};
+
+// The visibilities of one (u, v, w-bin) region, zero-padded to its count.
+struct VisBin {
+  WBin bin;
+  Vis vis;
+};
+
+// A complex grid region: dims (2, width, height), strides (1, 2, 2 width),
+// mins (0, min_u, min_v) (Data.hs:64-76, 93-97).
+struct UVGrid {
+  std::vector<double> data;
+  int min_u = 0, min_v = 0, width = 0, height = 0;
+};
+
+// GCFs: dims (2, S, S, 64) (Data.hs:125-133).
+struct GCFs {
+  std::vector<double> data;
+  int size = 0;
+};
+
+// A real image: dims (width, height), strides (1, width) (Data.hs:81-91).
+struct Image {
+  std::vector<double> data;
+  int width = 0, height = 0;
+};
+
+namespace detail {
+inline buffer_t make_buffer(double* host, std::initializer_list<int> ext,
+                            std::initializer_list<int> str, std::initializer_list<int> mins) {
+  buffer_t b{};
+  b.host = (uint8_t*)host;
+  int k = 0;
+  for (int e : ext) b.extent[k++] = e;
+  k = 0;
+  for (int s : str) b.stride[k++] = s;
+  k = 0;
+  for (int m : mins) b.min[k++] = m;
+  b.elem_size = 8;
+  b.host_dirty = true;
+  return b;
+}
+// Flow/Halide.hs:154-171: vis dims (5, N) plus the u/v placeholder dims
+inline buffer_t vis_buffer(Vis& v) {
+  return make_buffer(v.rec.data(), {5, (int)v.size(), 1, 1}, {1, 5, 0, 0}, {0, 0, 0, 0});
+}
+inline buffer_t gcf_buffer(GCFs& g) {
+  const int S = g.size;
+  return make_buffer(g.data.data(), {2, S, S, 64}, {1, 2, 2 * S, 2 * S * S}, {0, 0, 0, 0});
+}
+inline buffer_t uvg_buffer(UVGrid& g) {
+  return make_buffer(g.data.data(), {2, g.width, g.height}, {1, 2, 2 * g.width},
+                     {0, g.min_u, g.min_v});
+}
+inline buffer_t image_buffer(Image& im) {
+  return make_buffer(im.data.data(), {im.width, im.height}, {1, im.width}, {0, 0});
+}
+inline UVGrid zero_grid(int min_u, int min_v, int width, int height) {
+  UVGrid g;
+  g.min_u = min_u;
+  g.min_v = min_v;
+  g.width = width;
+  g.height = height;
+  g.data.assign((size_t)2 * width * height, 0.0);
+  return g;
+}
+}  // namespace detail
+
+// ------------------------------------------------------------ Kernel.Binning
+// binSizer (Binning.hs:34-99) for one (u, v) tile: the w range of the
+// visibilities inside the tile's u/v range (the fold starts from (0, 0)),
+// widened by 1e-4 of itself at the top, cut into gp.bins equal bins, and each
+// bin's count by bin = clamp(floor((w - low) / (high - low) * bins)).
+inline std::vector<WBin> binSizer(const GridPar& gp, const Vis& vis, Range u, Range v) {
+  const double umin = gridXY2UV(gp, u.low), umax = gridXY2UV(gp, u.high);
+  const double vmin = gridXY2UV(gp, v.low), vmax = gridXY2UV(gp, v.high);
+  auto inside = [&](const double* r) {
+    return r[0] >= umin && r[0] < umax && r[1] >= vmin && r[1] < vmax;
+  };
+  double low = 0, high0 = 0;
+  for (int64_t i = 0; i < vis.size(); i++) {
+    const double* r = &vis.rec[5 * i];
+    if (inside(r)) {
+      low = std::min(r[2], low);
+      high0 = std::max(r[2], high0);
+    }
+  }
+  const double high = high0 + (high0 - low) * 0.0001;
+  const int bins = gp.bins;
+  auto start = [&](int b) { return low + (double)b * (high - low) / (double)bins; };
+  std::vector<WBin> out(bins);
+  for (int b = 0; b < bins; b++) out[b] = WBin{start(b), start(b + 1), 0};
+  for (int64_t i = 0; i < vis.size(); i++) {
+    const double* r = &vis.rec[5 * i];
+    if (!(inside(r) && r[2] >= low && r[2] <= high)) continue;
+    // a zero-width range (every w equal) puts everything in bin 0
+    const double f = high > low ? std::floor((r[2] - low) / (high - low) * (double)bins) : 0.0;
+    const int b = (int)std::max(0.0, std::min((double)(bins - 1), f));
+    out[b].count++;
+  }
+  return out;
+}
+
+// binner (Binning.hs:102-181) for one (u, v) tile: each visibility inside the
+// tile goes to the bin with the largest low <= w, if w < that bin's high;
+// every bin is then padded with zero records to its count.
+inline std::vector<VisBin> binner(const GridPar& gp, const Vis& vis, Range u, Range v,
+                                  const std::vector<WBin>& bins) {
+  const double ul = gridXY2UV(gp, u.low), uh = gridXY2UV(gp, u.high);
+  const double vl = gridXY2UV(gp, v.low), vh = gridXY2UV(gp, v.high);
+  std::vector<VisBin> out(bins.size());
+  for (size_t b = 0; b < bins.size(); b++) out[b].bin = bins[b];
+  for (int64_t i = 0; i < vis.size(); i++) {
+    const double* r = &vis.rec[5 * i];
+    if (!(ul <= r[0] && r[0] < uh && vl <= r[1] && r[1] < vh)) continue;
+    int k = -1;  // Map.lookupLE over the bins' lows (the last of equal lows)
+    for (size_t b = 0; b < bins.size(); b++)
+      if (bins[b].low <= r[2] && (k < 0 || bins[b].low >= bins[k].low)) k = (int)b;
+    if (k < 0 || !(r[2] < bins[k].high)) continue;
+    out[k].vis.rec.insert(out[k].vis.rec.end(), r, r + 5);
+  }
+  for (VisBin& vb : out)
+    if (vb.vis.size() < vb.bin.count) vb.vis.rec.resize((size_t)5 * vb.bin.count, 0.0);
+  return out;
+}
+
+// ------------------------------------------------------------ Kernel.IO
+// gcfKernel (IO.hs:97-115): the GCF file gcfGet picks for the bin's w range,
+// read as size^2 * 64 complex doubles, conjugated when the range lies mostly
+// at negative w (low < -high).
+inline GCFs gcfKernel(const GCFPar& p, const WBin& bin) {
+  const GCFFile& f = gcfGet(p, bin.low, bin.high);
+  GCFs g;
+  g.size = f.size;
+  g.data.resize((size_t)2 * f.size * f.size * 64);
+  FILE* fp = std::fopen(f.file.c_str(), "rb");
+  if (!fp) throw KernelError("gcfKernel: cannot open " + f.file, -1);
+  const size_t got = std::fread(g.data.data(), sizeof(double), g.data.size(), fp);
+  std::fclose(fp);
+  if (got != g.data.size()) throw KernelError("gcfKernel: short read of " + f.file, -1);
+  if (bin.low < -bin.high)
+    for (size_t i = 1; i < g.data.size(); i += 2) g.data[i] = -g.data[i];
+  return g;
+}
+
+// ------------------------------------------------------------ Kernel.Gridder
+// gridInit (Gridder.hs:25-27): the tile with a margin of gcfMaxSize / 2 on
+// every side (Data.hs:71-76), zeroed by kern_init.
+inline UVGrid gridInit(const GCFPar& gcfp, Range u, Range v) {
+  const int m = gcfMaxSize(gcfp) / 2;
+  UVGrid g = detail::zero_grid(u.low - m, v.low - m, u.size() + 2 * m, v.size() + 2 * m);
+  buffer_t b = detail::uvg_buffer(g);
+  check(kern_init(&b), "gridInit");
+  return g;
+}
+
+// gridKernel (Gridder.hs:30-43): grid += vis * gcf through the symbol of the
+// kernel type, bound to (gridScale, gridHeight, gcfMaxSize).
+inline void gridKernel(GridKernelType kt, const GridPar& gp, const GCFPar& gcfp, VisBin& vb,
+                       GCFs& gcf, UVGrid& grid) {
+  buffer_t bv = detail::vis_buffer(vb.vis), bg = detail::gcf_buffer(gcf),
+           bu = detail::uvg_buffer(grid);
+  const double scale = gridScale(gp);
+  const int32_t gs = gp.height, margin = gcfMaxSize(gcfp);
+  switch (kt) {
+    case GridKernelType::CPU:
+      check(kern_scatter(scale, gs, margin, &bv, &bg, &bu), "kern_scatter");
+      break;
+    case GridKernelType::GPU:
+      check(kern_scatter_gpu1(scale, gs, margin, &bv, &bg, &bu), "kern_scatter_gpu1");
+      break;
+    case GridKernelType::NV:
+      check(nvGridder(scale, gs, margin, &bv, &bg, &bu), "nvGridder");
+      break;
+  }
+}
+
+// gridInitDetile (Gridder.hs:76-77): the full grid without margins, zeroed.
+inline UVGrid gridInitDetile(Range u, Range v) {
+  UVGrid g = detail::zero_grid(u.low, v.low, u.size(), v.size());
+  buffer_t b = detail::uvg_buffer(g);
+  check(kern_init(&b), "gridInitDetile");
+  return g;
+}
+
+// gridDetiling (Gridder.hs:81-85): full += tile over their overlap.
+inline void gridDetiling(UVGrid& tile, UVGrid& full) {
+  buffer_t bi = detail::uvg_buffer(tile), bo = detail::uvg_buffer(full);
+  check(kern_detile(&bi, &bo), "gridDetiling");
+}
+
+// ------------------------------------------------------------ Kernel.Degrid
+// degridKernel (Degrid.hs:34-47): vis_out = vis - sum grid * gcf over the full
+// grid, through the symbol of the kernel type.
+inline Vis degridKernel(DegridKernelType kt, const GridPar& gp, const GCFPar& gcfp, GCFs& gcf,
+                        UVGrid& full, Vis& vis) {
+  Vis out;
+  out.rec.assign(vis.rec.size(), 0.0);
+  buffer_t bg = detail::gcf_buffer(gcf), bu = detail::uvg_buffer(full),
+           bv = detail::vis_buffer(vis), bo = detail::vis_buffer(out);
+  const double scale = gridScale(gp);
+  const int32_t gs = gp.height, margin = gcfMaxSize(gcfp);
+  if (kt == DegridKernelType::CPU)
+    check(kern_degrid(scale, gs, margin, &bg, &bu, &bv, &bo), "kern_degrid");
+  else
+    check(kern_degrid_gpu1(scale, gs, margin, &bg, &bu, &bv, &bo), "kern_degrid_gpu1");
+  return out;
+}
+
+// ------------------------------------------------------------ Kernel.FFT
+#ifndef GB_MS5_ABI
+// ifftKern (FFT.hs:18-20): grid -> facet image (kern_ifft; the facet is
+// width x height, Data.hs:81-85).
+inline Image ifftKern(const GridPar& gp, UVGrid& full) {
+  Image im;
+  im.width = gp.width;
+  im.height = gp.height;
+  im.data.assign((size_t)im.width * im.height, 0.0);
+  buffer_t bu = detail::uvg_buffer(full), bi = detail::image_buffer(im);
+  check(kern_ifft(&bu, &bi), "kern_ifft");
+  return im;
+}
+
+// fftKern (FFT.hs:14-16): image -> full grid (kern_fft; both of the image size,
+// Data.hs:87-97).
+inline UVGrid fftKern(const GridPar& gp, Image& im) {
+  UVGrid g = detail::zero_grid(0, 0, gridImageWidth(gp), gridImageHeight(gp));
+  buffer_t bi = detail::image_buffer(im), bu = detail::uvg_buffer(g);
+  check(kern_fft(&bi, &bu), "kern_fft");
+  return g;
+}
+#endif
+
+}  // namespace rc

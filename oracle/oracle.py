@@ -159,6 +159,49 @@ def binsizer(w):
     return low, high0 + (high0 - low) * 0.0001
 
 
+def xy2uv(height, scale, z):
+    """gridXY2UV (MS6/programs/Kernel/Config.hs:211-212)."""
+    return float(z - height // 2) / scale
+
+
+def tile_bins(vis5, height, scale, u_range, v_range, bins):
+    """binSizer + binner (MS6/programs/Kernel/Binning.hs:34-99, 102-181) for one
+    (u, v) tile of pixel ranges [lo, hi): returns [(low, high, count, records)]
+    per w-bin, records padded with zero rows to count."""
+    vis5 = np.asarray(vis5, np.float64)
+    u, v, w = vis5[:, 0], vis5[:, 1], vis5[:, 2]
+    umin, umax = xy2uv(height, scale, u_range[0]), xy2uv(height, scale, u_range[1])
+    vmin, vmax = xy2uv(height, scale, v_range[0]), xy2uv(height, scale, v_range[1])
+    inside = (u >= umin) & (u < umax) & (v >= vmin) & (v < vmax)
+    low, high0 = 0.0, 0.0  # the fold's start
+    for x in w[inside]:
+        low, high0 = min(x, low), max(x, high0)
+    high = high0 + (high0 - low) * 0.0001
+    starts = [low + b * (high - low) / bins for b in range(bins + 1)]
+    counts = [0] * bins
+    for x in w[inside]:
+        if not (low <= x <= high):
+            continue
+        f = np.floor((x - low) / (high - low) * bins) if high > low else 0.0
+        counts[int(max(0, min(bins - 1, f)))] += 1
+    recs = [[] for _ in range(bins)]
+    for i in np.flatnonzero(inside):
+        x = w[i]
+        cand = [b for b in range(bins) if starts[b] <= x]  # Map.lookupLE on the lows
+        if not cand:
+            continue
+        k = max(cand, key=lambda b: (starts[b], b))
+        if x < starts[k + 1]:
+            recs[k].append(vis5[i])
+    out = []
+    for b in range(bins):
+        r = np.array(recs[b], np.float64).reshape(-1, 5)
+        if len(r) < counts[b]:
+            r = np.vstack([r, np.zeros((counts[b] - len(r), 5))])
+        out.append((starts[b], starts[b + 1], counts[b], r))
+    return out
+
+
 # ---------------------------------------------------------------- GCF generation (MS4 spec)
 def gcf_layers(w, support, max_support, t2, taper=None, over=OVER):
     """One w-plane's oversampled GCF in the MS6 layout [ou + 8*ov][sy][sx] (complex128).

@@ -1,0 +1,129 @@
+// The gridding strategy of MS6/programs/gridding.hs:40-103, restated on the
+// C++ host layer (include/rc_kernels.hpp) for the parity tests: for every
+// (u, v) tile, binSizer + binner, gridInit, one gridKernel per w-bin with
+// the bin's GCF (gcfKernel), gridDetiling into the full grid; then ifftKern.
+// With a model grid it also degrids every binned visibility (degridKernel),
+// as the continuum strategy does against its model.
+//
+// usage: gridding_strategy DIR MODE     MODE = bins | grid | degrid
+//   DIR/params.txt   width height theta tiles bins n_gcf grid_kernel degrid_kernel
+//                    then n_gcf lines "file size w"
+//   DIR/vis.bin      N x 5 doubles (u v w re im)
+//   DIR/model.bin    width x height complex doubles (degrid)
+// writes DIR/bins.bin (per tile, per bin: low high count, then the binned
+// records), DIR/grid.bin, DIR/image.bin, DIR/pred.bin (the degridded records
+// in tile, bin order).
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "rc_kernels.hpp"
+
+static std::vector<double> read_doubles(const std::string& path) {
+  std::vector<double> v;
+  FILE* f = std::fopen(path.c_str(), "rb");
+  if (!f) return v;
+  double x[4096];
+  size_t k;
+  while ((k = std::fread(x, sizeof(double), 4096, f)) > 0) v.insert(v.end(), x, x + k);
+  std::fclose(f);
+  return v;
+}
+
+static void write_doubles(const std::string& path, const std::vector<double>& v) {
+  FILE* f = std::fopen(path.c_str(), "wb");
+  if (!f) throw rc::KernelError("cannot write " + path, -1);
+  std::fwrite(v.data(), sizeof(double), v.size(), f);
+  std::fclose(f);
+}
+
+int main(int argc, char** argv) {
+  if (argc < 3) {
+    std::fprintf(stderr, "usage: %s DIR bins|grid|degrid\n", argv[0]);
+    return 2;
+  }
+  const std::string dir = argv[1], mode = argv[2];
+  try {
+    rc::GridPar gp;
+    rc::GCFPar gcfp;
+    int n_gcf = 0, gk = 1, dk = 1;
+    FILE* pf = std::fopen((dir + "/params.txt").c_str(), "r");
+    if (!pf || std::fscanf(pf, "%d %d %lf %d %d %d %d %d", &gp.width, &gp.height, &gp.theta,
+                           &gp.tiles, &gp.bins, &n_gcf, &gk, &dk) != 8)
+      throw rc::KernelError("bad params.txt", -1);
+    gp.pitch = gp.width;
+    for (int i = 0; i < n_gcf; i++) {
+      char name[4096];
+      rc::GCFFile f;
+      if (std::fscanf(pf, "%4095s %d %lf", name, &f.size, &f.w) != 3)
+        throw rc::KernelError("bad GCF line", -1);
+      f.file = name;
+      gcfp.files.push_back(f);
+    }
+    std::fclose(pf);
+    const auto gkt = gk == 0 ? rc::GridKernelType::CPU
+                     : gk == 1 ? rc::GridKernelType::GPU
+                               : rc::GridKernelType::NV;
+    const auto dkt = dk == 0 ? rc::DegridKernelType::CPU : rc::DegridKernelType::GPU;
+
+    rc::Vis vis;
+    vis.rec = read_doubles(dir + "/vis.bin");
+    rc::UVGrid model;
+    if (mode == "degrid") {
+      model.width = gp.width;
+      model.height = gp.height;
+      model.data = read_doubles(dir + "/model.bin");
+      if (model.data.size() != (size_t)2 * gp.width * gp.height)
+        throw rc::KernelError("bad model.bin", -1);
+    }
+
+    std::vector<double> bins_out, pred_out;
+    rc::UVGrid full;
+    if (mode == "grid") full = rc::gridInitDetile({0, gp.width}, {0, gp.height});
+    for (int tv = 0; tv < gp.tiles; tv++)
+      for (int tu = 0; tu < gp.tiles; tu++) {
+        // split of a range domain: low + (high - low) * i div n (Flow/Domain.hs:36-39)
+        const rc::Range u{tu * gp.width / gp.tiles, (tu + 1) * gp.width / gp.tiles};
+        const rc::Range v{tv * gp.height / gp.tiles, (tv + 1) * gp.height / gp.tiles};
+        const std::vector<rc::WBin> bins = rc::binSizer(gp, vis, u, v);
+        std::vector<rc::VisBin> vb = rc::binner(gp, vis, u, v, bins);
+        if (mode == "bins") {
+          for (const rc::VisBin& b : vb) {
+            bins_out.push_back(b.bin.low);
+            bins_out.push_back(b.bin.high);
+            bins_out.push_back((double)b.bin.count);
+            bins_out.push_back((double)b.vis.size());
+            bins_out.insert(bins_out.end(), b.vis.rec.begin(), b.vis.rec.end());
+          }
+          continue;
+        }
+        if (mode == "grid") {
+          rc::UVGrid tile = rc::gridInit(gcfp, u, v);
+          for (rc::VisBin& b : vb) {
+            if (b.vis.size() == 0) continue;
+            rc::GCFs g = rc::gcfKernel(gcfp, b.bin);
+            rc::gridKernel(gkt, gp, gcfp, b, g, tile);
+          }
+          rc::gridDetiling(tile, full);
+        } else {
+          for (rc::VisBin& b : vb) {
+            if (b.vis.size() == 0) continue;
+            rc::GCFs g = rc::gcfKernel(gcfp, b.bin);
+            const rc::Vis out = rc::degridKernel(dkt, gp, gcfp, g, model, b.vis);
+            pred_out.insert(pred_out.end(), out.rec.begin(), out.rec.end());
+          }
+        }
+      }
+    if (mode == "bins") write_doubles(dir + "/bins.bin", bins_out);
+    if (mode == "grid") {
+      write_doubles(dir + "/grid.bin", full.data);
+      const rc::Image im = rc::ifftKern(gp, full);
+      write_doubles(dir + "/image.bin", im.data);
+    }
+    if (mode == "degrid") write_doubles(dir + "/pred.bin", pred_out);
+  } catch (const rc::KernelError& e) {
+    std::fprintf(stderr, "%s\n", e.what());
+    return 1;
+  }
+  return 0;
+}

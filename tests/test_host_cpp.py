@@ -1,0 +1,56 @@
+"""The C++ host layer (include/rc_kernels.hpp) without a GPU: its binSizer and
+binner (MS6/programs/Kernel/Binning.hs:34-181) against the oracle's
+restatement, bit for bit, over a tiled grid with visibilities on tile edges,
+outside the grid, and a tile whose visibilities all have w = 0 (a zero-width
+w range: the reference counts them into bin 0 and its binner, whose bins all
+start at 0, drops them, so bin 0 is padded with zero records); and
+gcfKernel's error when no GCF file covers a bin (gcfGet, Config.hs:128-132)."""
+import numpy as np
+import pytest
+
+from tests import host_cpp as H
+
+G, THETA = 256, 0.05
+
+
+@pytest.fixture(scope="module")
+def exe(tmp_path_factory):
+    return H.build_program(tmp_path_factory.mktemp("cpp"))
+
+
+def test_binning_matches_the_oracle(exe, tmp_path):
+    vis5 = H.synthetic(1, 5000, G, THETA, 80.0)
+    # on tile edges (u = xy2uv of a boundary pixel), outside the grid, and a
+    # zero-w quarter: every visibility of the (0, 0) tile gets w = 0
+    edges = [H.O.xy2uv(G, THETA, z) for z in (0, 128, 256)]
+    vis5[:30, 0] = np.repeat(edges, 10)
+    vis5[30:40, 1] = 1e6
+    first = (vis5[:, 0] < edges[1]) & (vis5[:, 1] < edges[1])
+    vis5[first, 2] = 0.0
+    H.write_case(tmp_path, G, THETA, 2, 4, vis5, [(0.0, np.zeros((64, 8, 8), np.complex128))])
+    r = H.run(exe, tmp_path, "bins")
+    assert r.returncode == 0, r.stderr
+    got = np.fromfile(tmp_path / "bins.bin")
+    k = 0
+    zero_bin_seen = False
+    for tile in H.expected_bins(vis5, G, THETA, 2, 4):
+        for low, high, count, recs in tile:
+            assert got[k] == low and got[k + 1] == high and got[k + 2] == count
+            n = int(got[k + 3])
+            assert n == len(recs)
+            assert np.array_equal(got[k + 4:k + 4 + 5 * n].reshape(n, 5), recs)
+            zero_bin_seen |= low == high and count > 0 and not recs.any()
+            k += 4 + 5 * n
+    assert k == len(got)
+    assert zero_bin_seen
+
+
+def test_gcf_kernel_fails_like_gcfget(exe, tmp_path):
+    """GCF files only for w >= 50 and every w >= 0, so the first bin, [0, 20],
+    has none: the call fails there, before any GPU work."""
+    vis5 = H.synthetic(2, 500, G, THETA, 80.0)
+    vis5[:, 2] = np.abs(vis5[:, 2])
+    H.write_case(tmp_path, G, THETA, 1, 4, vis5, [(50.0, np.zeros((64, 8, 8), np.complex128))])
+    r = H.run(exe, tmp_path, "grid")
+    assert r.returncode == 1
+    assert "gcfGet" in r.stderr and "no GCF" in r.stderr
