@@ -319,6 +319,62 @@ inline Vis degridKernel(DegridKernelType kt, const GridPar& gp, const GCFPar& gc
   return out;
 }
 
+// ------------------------------------------------------------ Kernel.Cleaning
+// Config.hs:134-138
+struct CleanPar {
+  double gain = 0.1, threshold = 0;
+  int cycles = 0;
+};
+
+// psfVisKernel (Cleaning.hs:15-19): the visibilities with re = 1, im = 0.
+inline Vis psfVisKernel(Vis& vis) {
+  Vis out;
+  out.rec.assign(vis.rec.size(), 0.0);
+  buffer_t bi = detail::vis_buffer(vis), bo = detail::vis_buffer(out);
+  check(kern_psf_vis(&bi, &bo), "kern_psf_vis");
+  return out;
+}
+
+// cleanModel (Cleaning.hs:22-32): Hogbom CLEAN of `res` with `psf`,
+// accumulating into `model` (written in place, as halideKernel2Write does).
+inline void cleanModel(const CleanPar& cp, Image& psf, Image& res, Image& model) {
+  buffer_t bp = detail::image_buffer(psf), br = detail::image_buffer(res),
+           bm = detail::image_buffer(model);
+  check(kern_hogbom_model(cp.gain, cp.threshold, &bp, &br, &bm), "kern_hogbom_model");
+}
+
+// cleanResidual (Cleaning.hs:35-44): the residual image of the same CLEAN.
+inline Image cleanResidual(const CleanPar& cp, Image& psf, Image& res) {
+  Image out;
+  out.width = res.width;
+  out.height = res.height;
+  out.data.assign(res.data.size(), 0.0);
+  buffer_t bp = detail::image_buffer(psf), br = detail::image_buffer(res),
+           bo = detail::image_buffer(out);
+  check(kern_hogbom_residual(cp.gain, cp.threshold, &bp, &br, &bo), "kern_hogbom_residual");
+  return out;
+}
+
+// ------------------------------------------------------------ Kernel.Facet
+// rotateKernel (Facet.hs:19-54) for the facet of pixel ranges (l, m): phase
+// rotation of raw visibilities from the phase centre (lon, lat) to the
+// facet's centre, without uvw reprojection (the binding fixes doRep = False).
+inline Vis rotateKernel(const GridPar& gp, double lon, double lat, Range l, Range m, Vis& vis) {
+  const double facets = (double)gp.facets;
+  const double lon_incr = gp.theta / (double)gp.width / facets;  // radians per pixel
+  const double lat_incr = gp.theta / (double)gp.height / facets;
+  const double lon0 = lon - lon_incr * (double)(gridImageWidth(gp) / 2 - gp.width / 2);
+  const double lat0 = lat - lat_incr * (double)(gridImageHeight(gp) / 2 - gp.height / 2);
+  Vis out;
+  out.rec.assign(vis.rec.size(), 0.0);
+  buffer_t bi = detail::vis_buffer(vis);
+  // RotatedVisRepr (Data.hs:109-113): the facet's l / m region lows in dims 2 / 3
+  buffer_t bo = detail::make_buffer(out.rec.data(), {5, (int)out.size(), 1, 1}, {1, 5, 0, 0},
+                                    {0, 0, l.low, m.low});
+  check(kern_rotate(lon, lat, lon0, lat0, lon_incr, lat_incr, 0, &bi, &bo), "kern_rotate");
+  return out;
+}
+
 // ------------------------------------------------------------ Kernel.FFT
 #ifndef GB_MS5_ABI
 // ifftKern (FFT.hs:18-20): grid -> facet image (kern_ifft; the facet is

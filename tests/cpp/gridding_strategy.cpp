@@ -3,16 +3,21 @@
 // (u, v) tile, binSizer + binner, gridInit, one gridKernel per w-bin with
 // the bin's GCF (gcfKernel), gridDetiling into the full grid; then ifftKern.
 // With a model grid it also degrids every binned visibility (degridKernel),
-// as the continuum strategy does against its model.
+// as the continuum strategy does against its model; `clean` images the
+// visibilities and their PSF (psfVisKernel) and CLEANs (cleanModel,
+// cleanResidual); `rotate` phase-rotates them to a facet (rotateKernel).
 //
-// usage: gridding_strategy DIR MODE     MODE = bins | grid | degrid
+// usage: gridding_strategy DIR MODE     MODE = bins | grid | degrid | clean | rotate
 //   DIR/params.txt   width height theta tiles bins n_gcf grid_kernel degrid_kernel
 //                    then n_gcf lines "file size w"
 //   DIR/vis.bin      N x 5 doubles (u v w re im)
 //   DIR/model.bin    width x height complex doubles (degrid)
+//   DIR/clean.txt    gain threshold (clean)
+//   DIR/rotate.txt   facets lon lat l_low m_low (rotate)
 // writes DIR/bins.bin (per tile, per bin: low high count, then the binned
 // records), DIR/grid.bin, DIR/image.bin, DIR/pred.bin (the degridded records
-// in tile, bin order).
+// in tile, bin order), DIR/clean_model.bin + DIR/clean_residual.bin,
+// DIR/rot.bin.
 #include <cstdio>
 #include <string>
 #include <vector>
@@ -35,6 +40,27 @@ static void write_doubles(const std::string& path, const std::vector<double>& v)
   if (!f) throw rc::KernelError("cannot write " + path, -1);
   std::fwrite(v.data(), sizeof(double), v.size(), f);
   std::fclose(f);
+}
+
+// Tiles, bins, per-bin gridding, detiling (gridding.hs:58-97): the full grid.
+static rc::UVGrid grid_tiles(rc::GridKernelType kt, const rc::GridPar& gp, const rc::GCFPar& gcfp,
+                             const rc::Vis& vis) {
+  rc::UVGrid full = rc::gridInitDetile({0, gp.width}, {0, gp.height});
+  for (int tv = 0; tv < gp.tiles; tv++)
+    for (int tu = 0; tu < gp.tiles; tu++) {
+      // split of a range domain: low + (high - low) * i div n (Flow/Domain.hs:36-39)
+      const rc::Range u{tu * gp.width / gp.tiles, (tu + 1) * gp.width / gp.tiles};
+      const rc::Range v{tv * gp.height / gp.tiles, (tv + 1) * gp.height / gp.tiles};
+      std::vector<rc::VisBin> vb = rc::binner(gp, vis, u, v, rc::binSizer(gp, vis, u, v));
+      rc::UVGrid tile = rc::gridInit(gcfp, u, v);
+      for (rc::VisBin& b : vb) {
+        if (b.vis.size() == 0) continue;
+        rc::GCFs g = rc::gcfKernel(gcfp, b.bin);
+        rc::gridKernel(kt, gp, gcfp, b, g, tile);
+      }
+      rc::gridDetiling(tile, full);
+    }
+  return full;
 }
 
 int main(int argc, char** argv) {
@@ -77,9 +103,44 @@ int main(int argc, char** argv) {
         throw rc::KernelError("bad model.bin", -1);
     }
 
+    if (mode == "grid") {
+      rc::UVGrid full = grid_tiles(gkt, gp, gcfp, vis);
+      write_doubles(dir + "/grid.bin", full.data);
+      write_doubles(dir + "/image.bin", rc::ifftKern(gp, full).data);
+      return 0;
+    }
+    if (mode == "clean") {
+      rc::CleanPar cp;
+      FILE* cf = std::fopen((dir + "/clean.txt").c_str(), "r");
+      if (!cf || std::fscanf(cf, "%lf %lf", &cp.gain, &cp.threshold) != 2)
+        throw rc::KernelError("bad clean.txt", -1);
+      std::fclose(cf);
+      rc::UVGrid g_dirty = grid_tiles(gkt, gp, gcfp, vis);
+      rc::Image dirty = rc::ifftKern(gp, g_dirty);
+      rc::Vis psf_vis = rc::psfVisKernel(vis);
+      rc::UVGrid g_psf = grid_tiles(gkt, gp, gcfp, psf_vis);
+      rc::Image psf = rc::ifftKern(gp, g_psf);
+      rc::Image model = dirty;
+      std::fill(model.data.begin(), model.data.end(), 0.0);
+      rc::cleanModel(cp, psf, dirty, model);
+      write_doubles(dir + "/clean_model.bin", model.data);
+      write_doubles(dir + "/clean_residual.bin", rc::cleanResidual(cp, psf, dirty).data);
+      return 0;
+    }
+    if (mode == "rotate") {
+      double lon = 0, lat = 0;
+      int l_low = 0, m_low = 0;
+      FILE* rf = std::fopen((dir + "/rotate.txt").c_str(), "r");
+      if (!rf || std::fscanf(rf, "%d %lf %lf %d %d", &gp.facets, &lon, &lat, &l_low, &m_low) != 5)
+        throw rc::KernelError("bad rotate.txt", -1);
+      std::fclose(rf);
+      const rc::Vis out = rc::rotateKernel(gp, lon, lat, {l_low, l_low + gp.width},
+                                           {m_low, m_low + gp.height}, vis);
+      write_doubles(dir + "/rot.bin", out.rec);
+      return 0;
+    }
+
     std::vector<double> bins_out, pred_out;
-    rc::UVGrid full;
-    if (mode == "grid") full = rc::gridInitDetile({0, gp.width}, {0, gp.height});
     for (int tv = 0; tv < gp.tiles; tv++)
       for (int tu = 0; tu < gp.tiles; tu++) {
         // split of a range domain: low + (high - low) * i div n (Flow/Domain.hs:36-39)
@@ -97,29 +158,14 @@ int main(int argc, char** argv) {
           }
           continue;
         }
-        if (mode == "grid") {
-          rc::UVGrid tile = rc::gridInit(gcfp, u, v);
-          for (rc::VisBin& b : vb) {
-            if (b.vis.size() == 0) continue;
-            rc::GCFs g = rc::gcfKernel(gcfp, b.bin);
-            rc::gridKernel(gkt, gp, gcfp, b, g, tile);
-          }
-          rc::gridDetiling(tile, full);
-        } else {
-          for (rc::VisBin& b : vb) {
-            if (b.vis.size() == 0) continue;
-            rc::GCFs g = rc::gcfKernel(gcfp, b.bin);
-            const rc::Vis out = rc::degridKernel(dkt, gp, gcfp, g, model, b.vis);
-            pred_out.insert(pred_out.end(), out.rec.begin(), out.rec.end());
-          }
+        for (rc::VisBin& b : vb) {  // degrid
+          if (b.vis.size() == 0) continue;
+          rc::GCFs g = rc::gcfKernel(gcfp, b.bin);
+          const rc::Vis out = rc::degridKernel(dkt, gp, gcfp, g, model, b.vis);
+          pred_out.insert(pred_out.end(), out.rec.begin(), out.rec.end());
         }
       }
     if (mode == "bins") write_doubles(dir + "/bins.bin", bins_out);
-    if (mode == "grid") {
-      write_doubles(dir + "/grid.bin", full.data);
-      const rc::Image im = rc::ifftKern(gp, full);
-      write_doubles(dir + "/image.bin", im.data);
-    }
     if (mode == "degrid") write_doubles(dir + "/pred.bin", pred_out);
   } catch (const rc::KernelError& e) {
     std::fprintf(stderr, "%s\n", e.what());

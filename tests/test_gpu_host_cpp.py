@@ -4,8 +4,10 @@ against the same strategy composed from the oracle: per (u, v) tile, the
 oracle's binSizer + binner, kern_scatter semantics per w-bin with the GCF
 that gcfGet picks (conjugated for negative w) into the tile with its margin,
 detiling into the full grid; then kern_ifft.  And degridding every binned
-visibility against the model grid.  All within relative L2 1e-12 (FP64);
-u, v, w of the predictions exact."""
+visibility against the model grid; imaging the visibilities and their PSF
+and CLEANing (psfVisKernel, cleanModel, cleanResidual); phase rotation to a
+facet (rotateKernel).  All within relative L2 1e-12 (FP64); u, v, w of the
+predictions exact."""
 import numpy as np
 import pytest
 
@@ -38,12 +40,8 @@ def _gcf_for(gcfs, low, high):
     return np.conj(g) if conj else g
 
 
-@pytest.mark.parametrize("kernel", [1, 0, 2])  # kern_scatter_gpu1, kern_scatter, nvGridder
-def test_gridding_strategy(case, kernel):
-    exe, d, vis5, gcfs, model = case
-    H.write_case(d, G, THETA, TILES, BINS, vis5, gcfs, gk=kernel)
-    r = H.run(exe, d, "grid")
-    assert r.returncode == 0, r.stderr
+def oracle_grid(vis5, gcfs):
+    """The strategy composed from the oracle: the full grid and the records used."""
     m = max(S for _, S in W_FILES)  # gcfMaxSize: the margin argument
     full = np.zeros((G, G), np.complex128)
     used = 0
@@ -57,6 +55,16 @@ def test_gridding_strategy(case, kernel):
                 O.scatter(THETA, G, m, recs, _gcf_for(gcfs, low, high), tile, mx, my)
                 used += len(recs)
             full = O.detile(tile, (mx, my), full, (0, 0))
+    return full, used
+
+
+@pytest.mark.parametrize("kernel", [1, 0, 2])  # kern_scatter_gpu1, kern_scatter, nvGridder
+def test_gridding_strategy(case, kernel):
+    exe, d, vis5, gcfs, model = case
+    H.write_case(d, G, THETA, TILES, BINS, vis5, gcfs, gk=kernel)
+    r = H.run(exe, d, "grid")
+    assert r.returncode == 0, r.stderr
+    full, used = oracle_grid(vis5, gcfs)
     assert used > 0.9 * len(vis5)
     got = np.fromfile(d / "grid.bin").view(np.complex128).reshape(G, G)
     assert np.abs(full).max() > 0
@@ -83,3 +91,38 @@ def test_degridding_strategy(case, kernel):
     assert got.shape == exp.shape
     assert np.array_equal(got[:, :3], exp[:, :3])
     assert rel_l2(got[:, 3:], exp[:, 3:]) < TOL64
+
+
+def test_imaging_and_clean(case):
+    exe, d, vis5, gcfs, model = case
+    H.write_case(d, G, THETA, TILES, BINS, vis5, gcfs)
+    (d / "clean.txt").write_text("0.1 0.0\n")
+    r = H.run(exe, d, "clean")
+    assert r.returncode == 0, r.stderr
+    dirty = O.kern_ifft(oracle_grid(vis5, gcfs)[0])
+    psf5 = vis5.copy()
+    psf5[:, 3], psf5[:, 4] = 1.0, 0.0
+    psf = O.kern_ifft(oracle_grid(psf5, gcfs)[0])
+    em, er = O.hogbom_reference(0.1, 0.0, psf, dirty, np.zeros_like(dirty))
+    got_m = np.fromfile(d / "clean_model.bin").reshape(G, G)
+    got_r = np.fromfile(d / "clean_residual.bin").reshape(G, G)
+    assert np.abs(em).max() > 0
+    assert rel_l2(got_m, em) < TOL64
+    assert rel_l2(got_r, er) < TOL64
+
+
+def test_rotate_to_a_facet(case):
+    exe, d, vis5, gcfs, model = case
+    H.write_case(d, G, THETA, TILES, BINS, vis5, gcfs)
+    facets, lon, lat, l_low, m_low = 3, 1.2, -0.52, 1024, 2048
+    (d / "rotate.txt").write_text("%d %.17g %.17g %d %d\n" % (facets, lon, lat, l_low, m_low))
+    r = H.run(exe, d, "rotate")
+    assert r.returncode == 0, r.stderr
+    # Facet.hs:38-42
+    lon_incr, lat_incr = THETA / G / facets, THETA / G / facets
+    lon0 = lon - lon_incr * ((G * facets) // 2 - G // 2)
+    lat0 = lat - lat_incr * ((G * facets) // 2 - G // 2)
+    exp = O.rotate(lon, lat, lon0 + l_low * lon_incr, lat0 + m_low * lat_incr, 0, vis5)
+    got = np.fromfile(d / "rot.bin").reshape(-1, 5)
+    assert np.array_equal(got[:, :3], vis5[:, :3])
+    assert rel_l2(got[:, 3:], exp[:, 3:]) < 1e-11  # the kern_rotate bar (test_gpu_facet.py)
