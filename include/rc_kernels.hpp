@@ -28,6 +28,7 @@
 #include <vector>
 
 #include "rc_gb300.h"
+#include "rc_oskar.h"
 
 namespace rc {
 
@@ -253,6 +254,83 @@ inline GCFs gcfKernel(const GCFPar& p, const WBin& bin) {
   if (bin.low < -bin.high)
     for (size_t i = 1; i < g.data.size(); i += 2) g.data[i] = -g.data[i];
   return g;
+}
+
+// The reader's task data (MS6/kernel/oskar/OskarReader.hs:45-80): the file's
+// counts and its reshuffled arrays, amplitudes [baseline][time][channel][pol]
+// as complex doubles, u,v,w [baseline][time][channel][3] in wavelengths.
+struct TaskData {
+  int baselines = 0, times = 0, channels = 0, points = 0;
+  Metrix metrix{};
+  std::vector<WMaxMin> bl_max_min;
+  std::vector<double> vis;  // points x 4 complex
+  std::vector<double> uvws;  // points x 3
+  // tdVisibilityPtr / tdUVWPtr (OskarReader.hs:64-80); the u,v,w address
+  // ignores the channel stride, as there.
+  const double* visibility(int bl, int t, int ch, int pol) const {
+    return &vis[2 * ((size_t)pol + 4 * ((size_t)ch + (size_t)channels * (t + (size_t)times * bl)))];
+  }
+  const double* uvw(int bl, int t, int o) const {
+    return &uvws[(size_t)o + 3 * ((size_t)t + (size_t)times * bl)];
+  }
+};
+
+// readOskarData (OskarReader.hs:96-131): mkFromFile, readAndReshuffle,
+// freeBinHandler; a non-zero status throws with the reader's message.
+inline TaskData readOskarData(const std::string& fname) {
+  VisData vd;
+  const int st = mkFromFile(&vd, fname.c_str());
+  if (st != 0)
+    throw KernelError("While trying to read binary file " + fname + " : " + std::to_string(st), st);
+  TaskData td;
+  td.baselines = vd.num_baselines;
+  td.times = vd.num_times;
+  td.channels = vd.num_channels;
+  td.points = vd.num_points;
+  td.bl_max_min.resize(td.baselines);
+  td.vis.resize((size_t)td.points * 8);
+  td.uvws.resize((size_t)td.points * 3);
+  const int rd = readAndReshuffle(&vd, td.vis.data(), td.uvws.data(), &td.metrix,
+                                  td.bl_max_min.data());
+  freeBinHandler(&vd);
+  if (rd != 0)
+    throw KernelError("While trying to read binary file " + fname + " : " + std::to_string(rd), rd);
+  return td;
+}
+
+// oskarReader (MS6/programs/Kernel/IO.hs:22-74): 5-double records of points
+// [low, high) of one channel and polarisation, [baseline][time] order; the
+// region must lie inside the file and start on a baseline, as there.  Two
+// differences, both on input the Haskell kernel would read or write out of
+// bounds with: freq == channels (its check is freq > channels) and a pol
+// outside 0..3 are rejected, and a high that is not baseline-aligned ends the
+// records there (the Haskell kernel writes whole baselines past it).
+inline Vis oskarReader(const TaskData& td, int freq, int pol, int64_t low, int64_t high) {
+  if (freq < 0 || freq >= td.channels)
+    throw KernelError("Attempted to read non-existent frequency channel from Oskar data!", -1);
+  if (pol < 0 || pol > 3) throw KernelError("oskarReader: polarisation out of range", -1);
+  const int64_t total = (int64_t)td.times * td.baselines;
+  if (low < 0 || high > total)
+    throw KernelError("oskarReader: region out of bounds: " + std::to_string(low) + "-" +
+                          std::to_string(high) + " (only have " + std::to_string(total) +
+                          " points)",
+                      -1);
+  if (td.times == 0 || low % td.times != 0)
+    throw KernelError("oskarReader: region not baseline-aligned: " + std::to_string(low) + "-" +
+                          std::to_string(high),
+                      -1);
+  Vis out;
+  out.rec.reserve((size_t)5 * std::max<int64_t>(0, high - low));
+  for (int64_t i = low; i < high; i++) {
+    const int bl = (int)(i / td.times), t = (int)(i % td.times);
+    out.rec.push_back(*td.uvw(bl, t, 0));
+    out.rec.push_back(*td.uvw(bl, t, 1));
+    out.rec.push_back(*td.uvw(bl, t, 2));
+    const double* v = td.visibility(bl, t, freq, pol);
+    out.rec.push_back(v[0]);
+    out.rec.push_back(v[1]);
+  }
+  return out;
 }
 
 // ------------------------------------------------------------ Kernel.Gridder

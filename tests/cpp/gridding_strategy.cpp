@@ -5,19 +5,21 @@
 // With a model grid it also degrids every binned visibility (degridKernel),
 // as the continuum strategy does against its model; `clean` images the
 // visibilities and their PSF (psfVisKernel) and CLEANs (cleanModel,
-// cleanResidual); `rotate` phase-rotates them to a facet (rotateKernel).
+// cleanResidual); `rotate` phase-rotates them to a facet (rotateKernel);
+// `oskar` reads an OSKAR file's records (readOskarData, oskarReader).
 //
-// usage: gridding_strategy DIR MODE     MODE = bins | grid | degrid | clean | rotate
+// usage: gridding_strategy DIR MODE     MODE = bins | grid | degrid | clean | rotate | oskar
 //   DIR/params.txt   width height theta tiles bins n_gcf grid_kernel degrid_kernel
 //                    then n_gcf lines "file size w"
 //   DIR/vis.bin      N x 5 doubles (u v w re im)
 //   DIR/model.bin    width x height complex doubles (degrid)
 //   DIR/clean.txt    gain threshold (clean)
 //   DIR/rotate.txt   facets lon lat l_low m_low (rotate)
+//   DIR/oskar.txt    file freq pol low high (oskar)
 // writes DIR/bins.bin (per tile, per bin: low high count, then the binned
 // records), DIR/grid.bin, DIR/image.bin, DIR/pred.bin (the degridded records
 // in tile, bin order), DIR/clean_model.bin + DIR/clean_residual.bin,
-// DIR/rot.bin.
+// DIR/rot.bin, DIR/oskar.bin.
 #include <cstdio>
 #include <string>
 #include <vector>
@@ -70,6 +72,18 @@ int main(int argc, char** argv) {
   }
   const std::string dir = argv[1], mode = argv[2];
   try {
+    if (mode == "oskar") {
+      char name[4096];
+      int freq = 0, pol = 0;
+      long long low = 0, high = 0;
+      FILE* of = std::fopen((dir + "/oskar.txt").c_str(), "r");
+      if (!of || std::fscanf(of, "%4095s %d %d %lld %lld", name, &freq, &pol, &low, &high) != 5)
+        throw rc::KernelError("bad oskar.txt", -1);
+      std::fclose(of);
+      const rc::TaskData td = rc::readOskarData(name);
+      write_doubles(dir + "/oskar.bin", rc::oskarReader(td, freq, pol, low, high).rec);
+      return 0;
+    }
     rc::GridPar gp;
     rc::GCFPar gcfp;
     int n_gcf = 0, gk = 1, dk = 1;

@@ -126,3 +126,39 @@ def test_rotate_to_a_facet(case):
     got = np.fromfile(d / "rot.bin").reshape(-1, 5)
     assert np.array_equal(got[:, :3], vis5[:, :3])
     assert rel_l2(got[:, 3:], exp[:, 3:]) < 1e-11  # the kern_rotate bar (test_gpu_facet.py)
+
+
+@pytest.mark.parametrize("freq,pol,low,high", [(0, 0, 0, 70), (1, 3, 14, 63), (1, 2, 7, 8)])
+def test_oskar_reader(tmp_path, freq, pol, low, high):
+    """readOskarData + oskarReader on the committed golden file (10 baselines,
+    7 times, 2 channels), against the oracle's records of the reference
+    reader's own arrays (tests/golden/oskar_small_ref.npz), with the u,v,w
+    address of Kernel/IO.hs."""
+    import os
+
+    from oracle import oskar as K
+
+    exe = H.build_program(tmp_path)
+    path = os.path.join(H.ROOT, "tests", "golden", "oskar_small.vis")
+    (tmp_path / "oskar.txt").write_text("%s %d %d %d %d\n" % (path, freq, pol, low, high))
+    r = H.run(exe, tmp_path, "oskar")
+    assert r.returncode == 0, r.stderr
+    ref = np.load(os.path.join(H.ROOT, "tests", "golden", "oskar_small_ref.npz"))
+    exp = K.records(ref["amps"], ref["uvw"], 7, 2, freq, pol, low, high, True)
+    got = np.fromfile(tmp_path / "oskar.bin").reshape(-1, 5)
+    assert np.array_equal(got, exp)
+
+
+def test_oskar_reader_rejects_bad_regions(tmp_path):
+    import os
+
+    exe = H.build_program(tmp_path)
+    path = os.path.join(H.ROOT, "tests", "golden", "oskar_small.vis")
+    for args, msg in [((2, 0, 0, 7), "non-existent frequency"), ((0, 0, 3, 10), "baseline-aligned"),
+                      ((0, 0, 0, 71), "out of bounds")]:
+        (tmp_path / "oskar.txt").write_text("%s %d %d %d %d\n" % ((path,) + args))
+        r = H.run(exe, tmp_path, "oskar")
+        assert r.returncode == 1 and msg in r.stderr, r.stderr
+    (tmp_path / "oskar.txt").write_text("%s 0 0 0 7\n" % os.path.join(str(tmp_path), "none.vis"))
+    r = H.run(exe, tmp_path, "oskar")
+    assert r.returncode == 1 and "While trying to read binary file" in r.stderr
