@@ -16,6 +16,11 @@
 //                           for each bin b: gridKernel(kt, gp, gcfp, vb[b], gcfKernel(gcfp, b.bin), tile)
 //                           gridDetiling(tile, full)            (full = gridInitDetile(...))
 //   image = ifftKern(gp, full)
+//
+// Built with -DGB_MS5_ABI (against librc_gb300_ms5.so) the CPU gridder binds
+// MS5's kern_scatter, which takes no margin (MS5/programs/Kernel/Gridder.hs:
+// 28-35), and ifftKern binds MS5's kern_fft (MS5/programs/Kernel/FFT.hs:15-16);
+// MS5 has no fftKern.
 #pragma once
 
 #include <stdint.h>
@@ -28,6 +33,7 @@
 #include <vector>
 
 #include "rc_gb300.h"
+#include "rc_gb300_ms5.h"
 #include "rc_oskar.h"
 
 namespace rc {
@@ -354,7 +360,11 @@ inline void gridKernel(GridKernelType kt, const GridPar& gp, const GCFPar& gcfp,
   const int32_t gs = gp.height, margin = gcfMaxSize(gcfp);
   switch (kt) {
     case GridKernelType::CPU:
+#ifdef GB_MS5_ABI
+      check(kern_scatter(scale, gs, &bv, &bg, &bu), "kern_scatter");
+#else
       check(kern_scatter(scale, gs, margin, &bv, &bg, &bu), "kern_scatter");
+#endif
       break;
     case GridKernelType::GPU:
       check(kern_scatter_gpu1(scale, gs, margin, &bv, &bg, &bu), "kern_scatter_gpu1");
@@ -454,19 +464,23 @@ inline Vis rotateKernel(const GridPar& gp, double lon, double lat, Range l, Rang
 }
 
 // ------------------------------------------------------------ Kernel.FFT
-#ifndef GB_MS5_ABI
 // ifftKern (FFT.hs:18-20): grid -> facet image (kern_ifft; the facet is
-// width x height, Data.hs:81-85).
+// width x height, Data.hs:81-85).  MS5: its kern_fft, grid -> image.
 inline Image ifftKern(const GridPar& gp, UVGrid& full) {
   Image im;
   im.width = gp.width;
   im.height = gp.height;
   im.data.assign((size_t)im.width * im.height, 0.0);
   buffer_t bu = detail::uvg_buffer(full), bi = detail::image_buffer(im);
+#ifdef GB_MS5_ABI
+  check(kern_fft(&bu, &bi), "kern_fft");
+#else
   check(kern_ifft(&bu, &bi), "kern_ifft");
+#endif
   return im;
 }
 
+#ifndef GB_MS5_ABI
 // fftKern (FFT.hs:14-16): image -> full grid (kern_fft; both of the image size,
 // Data.hs:87-97).
 inline UVGrid fftKern(const GridPar& gp, Image& im) {

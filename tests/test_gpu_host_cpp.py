@@ -162,3 +162,31 @@ def test_oskar_reader_rejects_bad_regions(tmp_path):
     (tmp_path / "oskar.txt").write_text("%s 0 0 0 7\n" % os.path.join(str(tmp_path), "none.vis"))
     r = H.run(exe, tmp_path, "oskar")
     assert r.returncode == 1 and "While trying to read binary file" in r.stderr
+
+
+def test_ms5_gridding_strategy(tmp_path):
+    """The same strategy against librc_gb300_ms5.so (-DGB_MS5_ABI): the CPU
+    gridder type binds MS5's kern_scatter (no margin argument; GCF size 16, so
+    gcfMaxSize = 16 and the tiles' margins are MS5's), and ifftKern binds MS5's
+    kern_fft, 2n times MS6's kern_ifft, at 2048^2."""
+    g2, files = 2048, [(0.0, 16), (30.0, 16), (80.0, 16)]
+    exe = H.build_program(tmp_path, ms5=True)
+    vis5 = H.synthetic(6, 12000, g2, THETA, 120.0)
+    gcfs = [(w, O.gcf_layers(w, S, 16, THETA / 2)) for w, S in files]
+    H.write_case(tmp_path, g2, THETA, TILES, 8, vis5, gcfs, gk=0)
+    r = H.run(exe, tmp_path, "grid")
+    assert r.returncode == 0, r.stderr
+    full = np.zeros((g2, g2), np.complex128)
+    for v in H.tiles_of(g2, TILES):
+        for u in H.tiles_of(g2, TILES):
+            tile = np.zeros((v[1] - v[0] + 16, u[1] - u[0] + 16), np.complex128)
+            mx, my = u[0] - 8, v[0] - 8
+            for low, high, count, recs in O.tile_bins(vis5, g2, THETA, u, v, 8):
+                if len(recs):
+                    O.scatter(THETA, g2, 16, recs, _gcf_for(gcfs, low, high), tile, mx, my)
+            full = O.detile(tile, (mx, my), full, (0, 0))
+    got = np.fromfile(tmp_path / "grid.bin").view(np.complex128).reshape(g2, g2)
+    assert np.abs(full).max() > 0
+    assert rel_l2(got, full) < TOL64
+    img = np.fromfile(tmp_path / "image.bin").reshape(g2, g2)
+    assert rel_l2(img, 2 * g2 * O.kern_ifft(full)) < TOL64

@@ -54,3 +54,24 @@ def test_gcf_kernel_fails_like_gcfget(exe, tmp_path):
     r = H.run(exe, tmp_path, "grid")
     assert r.returncode == 1
     assert "gcfGet" in r.stderr and "no GCF" in r.stderr
+
+
+@pytest.mark.parametrize("flags", [[], ["-DGB_MS5_ABI"]])
+def test_headers_compile_as_cxx17_and_c(tmp_path, flags):
+    """rc_kernels.hpp as C++17 (with the MS5 variant's declarations too), and
+    the C headers as plain C99, warning-free."""
+    import os
+    import subprocess
+
+    inc = os.path.join(H.ROOT, "include")
+    src = tmp_path / "t.cpp"
+    src.write_text('#include "rc_kernels.hpp"\n#include "rc_gb300_ms5.h"\nint main() { return 0; }\n')
+    r = subprocess.run(["g++", "-std=c++17", "-Wall", "-Wextra", "-Werror", "-fsyntax-only", "-I", inc,
+                        str(src)] + flags, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    csrc = tmp_path / "t.c"
+    csrc.write_text('#include "rc_gb300.h"\n#include "rc_oskar.h"\n#include "rc_gb300_ms5.h"\n'
+                    'int main(void) { return 0; }\n')
+    r = subprocess.run(["gcc", "-std=c99", "-Wall", "-Wextra", "-Werror", "-fsyntax-only", "-I", inc,
+                        str(csrc)] + flags, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
