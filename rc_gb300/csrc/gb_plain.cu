@@ -601,8 +601,9 @@ static int compat_scatter(const char* who, int size_err, double scale, int32_t g
   const int64_t row = grid_row_doubles(uvg);
   if (n == 0) return GB_OK;  // the grid is unchanged
   cudaStream_t s, s2;
-  cudaEvent_t ev;
-  if ((rc = stage_stream(&s)) || (rc = stage_aux(&s2, &ev))) return rc;
+  cudaEvent_t* evs;
+  if ((rc = stage_stream(&s)) || (rc = stage_aux(&s2, &evs))) return rc;
+  const cudaEvent_t ev = evs[0];
   void *d_vis, *d_gcf, *d_grid, *d_acc;
   const size_t gcf_bytes = (size_t)GB_PHASES * S * S * 16;
   const size_t grid_bytes = (size_t)W * H * 16;
@@ -687,12 +688,15 @@ static int compat_degrid(const char* who, int size_err, double scale, int32_t gr
                        (int64_t)GB_PHASES * S * S, (float4*)d_grid_df, (float4*)d_gcf_df, d_exps,
                        s)))
     return rc;
-  // in chunks of visibilities: a chunk's results go down on the second stream
-  // while the next chunk is degridded
+  // In chunks of visibilities: every chunk's kernel is queued first, each
+  // followed by its event; a chunk's results then go down on the second stream
+  // while the later chunks are degridded.  (A copy into pageable memory returns
+  // only when done, so a copy issued between two launches would hold back the
+  // second.)
   cudaStream_t s2;
-  cudaEvent_t ev;
-  if ((rc = stage_aux(&s2, &ev))) return rc;
-  const int chunks = n >= (1 << 18) ? 4 : 1;
+  cudaEvent_t* evs;
+  if ((rc = stage_aux(&s2, &evs))) return rc;
+  const int chunks = n >= (1 << 18) ? kAuxEvents : 1;
   for (int c = 0; c < chunks; c++) {
     const int64_t c0 = n * c / chunks, c1 = n * (c + 1) / chunks;
     int blocks;
@@ -701,8 +705,11 @@ static int compat_degrid(const char* who, int size_err, double scale, int32_t gr
         c1 - c0, (const double*)d_vis + 5 * c0, (const double2*)d_gcf, (const double2*)d_grid,
         (const float4*)d_gcf_df, (const float4*)d_grid_df, d_exps, (double*)d_out + 5 * c0, geo);
     GB_TRY_DRAIN(cudaGetLastError(), s, s2);
-    GB_TRY_DRAIN(cudaEventRecord(ev, s), s, s2);
-    GB_TRY_DRAIN(cudaStreamWaitEvent(s2, ev, 0), s, s2);
+    GB_TRY_DRAIN(cudaEventRecord(evs[c], s), s, s2);
+  }
+  for (int c = 0; c < chunks; c++) {
+    const int64_t c0 = n * c / chunks, c1 = n * (c + 1) / chunks;
+    GB_TRY_DRAIN(cudaStreamWaitEvent(s2, evs[c], 0), s, s2);
     GB_TRY_DRAIN(cudaMemcpyAsync((double*)vis_out->host + 5 * c0, (const double*)d_out + 5 * c0,
                                  (size_t)(c1 - c0) * 40, cudaMemcpyDeviceToHost, s2),
                  s, s2);

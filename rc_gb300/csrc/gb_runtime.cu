@@ -35,14 +35,16 @@ namespace gb {
 struct Staging {
   cudaStream_t stream = nullptr;
   cudaStream_t stream2 = nullptr;  // overlaps copies with kernels inside one call
-  cudaEvent_t event = nullptr;
+  cudaEvent_t events[kAuxEvents] = {};
   int device = -1;
   void* buf[kStageSlots] = {};
   size_t cap[kStageSlots] = {};
   void release_aux() {
-    if (event) cudaEventDestroy(event);
+    for (cudaEvent_t& e : events) {
+      if (e) cudaEventDestroy(e);
+      e = nullptr;
+    }
     if (stream2) cudaStreamDestroy(stream2);
-    event = nullptr;
     stream2 = nullptr;
   }
   ~Staging() {
@@ -79,15 +81,16 @@ int stage_stream(cudaStream_t* out) {
   return GB_OK;
 }
 
-int stage_aux(cudaStream_t* s2, cudaEvent_t* ev) {
+int stage_aux(cudaStream_t* s2, cudaEvent_t** ev) {
   cudaStream_t s;
   int rc;
   if ((rc = stage_stream(&s))) return rc;  // also drops the aux objects of another device
   if (!t_stage.stream2)
     GB_CUDA_TRY(cudaStreamCreateWithFlags(&t_stage.stream2, cudaStreamNonBlocking));
-  if (!t_stage.event) GB_CUDA_TRY(cudaEventCreateWithFlags(&t_stage.event, cudaEventDisableTiming));
+  for (cudaEvent_t& e : t_stage.events)
+    if (!e) GB_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   *s2 = t_stage.stream2;
-  *ev = t_stage.event;
+  *ev = t_stage.events;
   return GB_OK;
 }
 

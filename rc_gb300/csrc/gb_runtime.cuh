@@ -7,14 +7,15 @@
 namespace gb {
 
 constexpr int kStageSlots = 6;
+constexpr int kAuxEvents = 4;
 
 // Per-host-thread stream and grow-only device buffers used by the synchronous
 // reference-ABI entry points.
 int stage_stream(cudaStream_t* out);
 int stage_buffer(int slot, size_t bytes, void** out);
-// A second stream and an event of the same thread, for overlapping a call's
-// copies with its kernels.
-int stage_aux(cudaStream_t* s2, cudaEvent_t* ev);
+// A second stream and kAuxEvents events of the same thread, for overlapping a
+// call's copies with its kernels.
+int stage_aux(cudaStream_t* s2, cudaEvent_t** ev);
 
 int sm_count();
 
