@@ -75,3 +75,12 @@ def test_headers_compile_as_cxx17_and_c(tmp_path, flags):
     r = subprocess.run(["gcc", "-std=c99", "-Wall", "-Wextra", "-Werror", "-fsyntax-only", "-I", inc,
                         str(csrc)] + flags, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+def test_strategy_program_builds_against_both_libraries(tmp_path):
+    """The strategy program links against librc_gb300.so and, with
+    -DGB_MS5_ABI, against librc_gb300_ms5.so (MS5's bindings), warning-free."""
+    import os
+
+    for ms5 in (False, True):
+        assert os.path.exists(H.build_program(tmp_path, ms5=ms5))
