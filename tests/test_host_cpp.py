@@ -84,3 +84,26 @@ def test_strategy_program_builds_against_both_libraries(tmp_path):
 
     for ms5 in (False, True):
         assert os.path.exists(H.build_program(tmp_path, ms5=ms5))
+
+
+def test_binning_of_empty_tiles(exe, tmp_path):
+    """Visibilities in one quadrant only: the other tiles' w range stays
+    (0, 0) from the fold's start, every bin is empty and nothing is padded."""
+    vis5 = H.synthetic(3, 800, G, THETA, 60.0)
+    vis5[:, 0] = -np.abs(vis5[:, 0]) - 1.0
+    vis5[:, 1] = -np.abs(vis5[:, 1]) - 1.0
+    H.write_case(tmp_path, G, THETA, 2, 3, vis5, [(0.0, np.zeros((64, 8, 8), np.complex128))])
+    r = H.run(exe, tmp_path, "bins")
+    assert r.returncode == 0, r.stderr
+    got = np.fromfile(tmp_path / "bins.bin")
+    k = 0
+    empty = 0
+    for tile in H.expected_bins(vis5, G, THETA, 2, 3):
+        for low, high, count, recs in tile:
+            assert got[k] == low and got[k + 1] == high and got[k + 2] == count
+            n = int(got[k + 3])
+            assert n == len(recs)
+            assert np.array_equal(got[k + 4:k + 4 + 5 * n].reshape(n, 5), recs)
+            empty += low == 0.0 and high == 0.0 and count == 0 and n == 0
+            k += 4 + 5 * n
+    assert k == len(got) and empty == 9  # three empty tiles x three bins
