@@ -20,7 +20,16 @@
 // finds it as the previous call left it: the counters, histogram and cursors
 // that must start at zero are cleared by each call, and calls whose GPU work
 // overlaps (on different streams, or from different host threads) race on the
-// array and must be serialised by the caller.
+// array and must be serialised by the caller.  The cached address belongs to
+// the device's current context: after cudaDeviceReset on a device this entry
+// point is not valid there for the rest of the process.
+//
+// Unlike a plan, the records of a (thread-group class, tile) bin are placed by
+// an atomic cursor, so pieces of different periods within a bin are not kept
+// in period order.  The tiled kernel stays correct (a run ends at each change
+// of period, with a group barrier), but a mixed bin splits into more, shorter
+// runs than a plan's would, and the FP32 summation order can change from call
+// to call (results agree to FP32 rounding, not bit for bit).
 #include <algorithm>
 #include <mutex>
 
@@ -266,6 +275,14 @@ extern "C" int gb_grid_f32_noalloc(const gb_geometry* geo, int64_t n_vis, const 
       cap * cap > 8 * NT) {
     gb_set_error(GB_ERR_ARG, "gb_grid_f32_noalloc: unsupported tuning tile=%d threads=%d cap=%d",
                  T, NT, cap);
+    return GB_ERR_ARG;
+  }
+  // work items hold tile indices as int16 (the rule of gb_plan_create): a grid
+  // more than 32767 tiles wide or high is rejected before any GPU work
+  if (geo->ext_x > 32767 * (int64_t)T || geo->ext_y > 32767 * (int64_t)T) {
+    gb_set_error(GB_ERR_ARG,
+                 "gb_grid_f32_noalloc: grid extent %d x %d exceeds 32767 tiles of %d pixels",
+                 geo->ext_x, geo->ext_y, T);
     return GB_ERR_ARG;
   }
   // planes -> pieces, periods, classes (the rules of gb_plan_create)
