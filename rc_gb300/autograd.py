@@ -2,9 +2,12 @@
 
     grid = ImageToGrid.apply(image, taper)        # grid correction + centred FFT
     vis  = Degrid.apply(grid, plan, gcf)          # D = G^H (tiled FP32 or plain FP64)
+    grid = Grid.apply(vis, plan, gcf)             # G (the adjoint direction)
 
-Backward passes are the hand-written adjoints: Degrid's is the gridding
-kernel (G), ImageToGrid's is gb_grid_to_image (Re[C^-1 S F^H S]).  complex64
+Backward passes are the hand-written adjoints, through the C ABI's
+forward / backward entry points: Degrid's is the gridding kernel (G,
+gb_degrid_backward), Grid's the degridding kernel (D, gb_grid_backward),
+ImageToGrid's is gb_grid_to_image (Re[C^-1 S F^H S]).  complex64
 tensors run the FP32 tiled pair, complex128 the plain FP64 pair.  torch is
 used for device memory, streams and autograd bookkeeping only.
 """
@@ -70,25 +73,40 @@ def grid_to_image(grid, taper=None):
 
 
 class Degrid(torch.autograd.Function):
+    """pred = D grid through gb_degrid_forward; backward through
+    gb_degrid_backward (the gridding kernel, G = D^H)."""
+
     @staticmethod
     def forward(ctx, grid, plan, gcf):
         grid = grid.contiguous()
-        if grid.dtype == torch.complex64:
-            pred = plan.degrid(gcf, grid)
-        else:
-            pred = plan.degrid64(gcf, grid)
+        pred = plan.degrid_forward(gcf, grid)
         ctx.plan, ctx.gcf, ctx.shape, ctx.dtype = plan, gcf, grid.shape, grid.dtype
         return pred
 
     @staticmethod
     def backward(ctx, gp):
-        gp = gp.contiguous()
+        gp = gp.to(ctx.dtype).contiguous()
         out = torch.zeros(ctx.shape, dtype=ctx.dtype, device=gp.device)
-        if ctx.dtype == torch.complex64:
-            ctx.plan.grid(gp.to(torch.complex64), ctx.gcf, out)
-        else:
-            ctx.plan.grid64(gp.to(torch.complex128), ctx.gcf, out)
+        ctx.plan.degrid_backward(ctx.gcf, gp, out)
         return out, None, None
+
+
+class Grid(torch.autograd.Function):
+    """grid = G vis through gb_grid_forward (into a zeroed grid); backward
+    through gb_grid_backward (the degridding kernel, D = G^H)."""
+
+    @staticmethod
+    def forward(ctx, vis, plan, gcf):
+        vis = vis.contiguous()
+        grid = torch.zeros(plan.grid_shape, dtype=vis.dtype, device=vis.device)
+        plan.grid_forward(gcf, vis, grid)
+        ctx.plan, ctx.gcf, ctx.dtype = plan, gcf, vis.dtype
+        return grid
+
+    @staticmethod
+    def backward(ctx, gg):
+        gg = gg.to(ctx.dtype).contiguous()
+        return ctx.plan.grid_backward(ctx.gcf, gg), None, None
 
 
 def forward_model(image, taper, plan, gcf):

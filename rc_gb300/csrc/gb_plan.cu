@@ -631,3 +631,25 @@ extern "C" int gb_degrid_f64(gb_plan* P, const double* d_gcf, const double* d_gr
   if (P->dev.n_vis == 0) return GB_OK;
   return launch_degrid_plain64(P, d_gcf, d_grid, d_pred, mode, P->df, (cudaStream_t)stream);
 }
+
+// The FP64 pair under its forward / backward names (see gb_grid_forward).
+extern "C" int gb_grid_forward_f64(gb_plan* P, const double* d_gcf, const double* d_vis,
+                                   double* d_grid, void* stream) {
+  return gb_grid_f64(P, d_vis, d_gcf, d_grid, stream);
+}
+
+extern "C" int gb_grid_backward_f64(gb_plan* P, const double* d_gcf, const double* d_grid_grad,
+                                    double* d_vis_grad, void* stream) {
+  return gb_degrid_f64(P, d_gcf, d_grid_grad, d_vis_grad, 0, stream);
+}
+
+extern "C" int gb_degrid_forward_f64(gb_plan* P, const double* d_gcf, const double* d_grid,
+                                     double* d_pred, void* stream) {
+  return gb_degrid_f64(P, d_gcf, d_grid, d_pred, 0, stream);
+}
+
+extern "C" int gb_degrid_backward_f64(gb_plan* P, const double* d_gcf,
+                                      const double* d_pred_grad, double* d_grid_grad,
+                                      void* stream) {
+  return gb_grid_f64(P, d_pred_grad, d_gcf, d_grid_grad, stream);
+}

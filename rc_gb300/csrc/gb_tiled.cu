@@ -1065,6 +1065,16 @@ extern "C" int gb_degrid_backward(gb_plan* P, const float* d_gcf, const float* d
   return gb_grid_f32(P, d_pred_grad, d_gcf, d_grid_grad, stream);
 }
 
+extern "C" int gb_grid_forward(gb_plan* P, const float* d_gcf, const float* d_vis, float* d_grid,
+                               void* stream) {
+  return gb_grid_f32(P, d_vis, d_gcf, d_grid, stream);
+}
+
+extern "C" int gb_grid_backward(gb_plan* P, const float* d_gcf, const float* d_grid_grad,
+                                float* d_vis_grad, void* stream) {
+  return gb_degrid_f32(P, d_gcf, d_grid_grad, d_vis_grad, 0, stream);
+}
+
 // ---------------------------------------------------------------- bounds-checked build
 #ifdef GB_CHECKED
 __global__ void k_checked_selftest() {

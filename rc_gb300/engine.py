@@ -148,6 +148,60 @@ class Plan:
                                         int(mode), _stream(stream)), "gb_degrid_f64")
         return out
 
+    # -------------------------------------------------------------- forward / backward
+    # gb_grid_forward / _backward and gb_degrid_forward / _backward (and their
+    # _f64 forms): complex64 tensors take the FP32 tiled pair, complex128 the
+    # plain FP64 pair.
+    def _pair(self, name, *ts):
+        import torch
+
+        dt = ts[0].dtype
+        assert dt in (torch.complex64, torch.complex128)
+        assert all(t.dtype == dt and t.is_contiguous() for t in ts)
+        assert ts[0].numel() >= self.gcf_len, "GCF array shorter than the plan's layout"
+        fn = name if dt == torch.complex64 else name + "_f64"
+        return fn, getattr(self.L, fn)
+
+    def grid_forward(self, gcf, vis, grid, stream=None):
+        """grid += G vis."""
+        assert vis.numel() == self.n and grid.shape == self.grid_shape
+        name, fn = self._pair("gb_grid_forward", gcf, vis, grid)
+        _lib.check(fn(self.h, gcf.data_ptr(), vis.data_ptr(), grid.data_ptr(), _stream(stream)),
+                   name)
+        return grid
+
+    def grid_backward(self, gcf, grid_grad, out=None, stream=None):
+        """vis_grad = G^H grid_grad (overwrites out)."""
+        import torch
+
+        assert grid_grad.shape == self.grid_shape
+        if out is None:
+            out = torch.empty(self.n, dtype=grid_grad.dtype, device=grid_grad.device)
+        name, fn = self._pair("gb_grid_backward", gcf, grid_grad, out)
+        _lib.check(fn(self.h, gcf.data_ptr(), grid_grad.data_ptr(), out.data_ptr(),
+                      _stream(stream)), name)
+        return out
+
+    def degrid_forward(self, gcf, grid, out=None, stream=None):
+        """pred = D grid = G^H grid."""
+        import torch
+
+        assert grid.shape == self.grid_shape
+        if out is None:
+            out = torch.empty(self.n, dtype=grid.dtype, device=grid.device)
+        name, fn = self._pair("gb_degrid_forward", gcf, grid, out)
+        _lib.check(fn(self.h, gcf.data_ptr(), grid.data_ptr(), out.data_ptr(), _stream(stream)),
+                   name)
+        return out
+
+    def degrid_backward(self, gcf, pred_grad, grid_grad, stream=None):
+        """grid_grad += D^H pred_grad = G pred_grad."""
+        assert pred_grad.numel() == self.n and grid_grad.shape == self.grid_shape
+        name, fn = self._pair("gb_degrid_backward", gcf, pred_grad, grid_grad)
+        _lib.check(fn(self.h, gcf.data_ptr(), pred_grad.data_ptr(), grid_grad.data_ptr(),
+                      _stream(stream)), name)
+        return grid_grad
+
     def close(self):
         if getattr(self, "h", None):
             self.L.gb_plan_destroy(self.h)

@@ -142,6 +142,12 @@ SIGNATURES = {
     "gb_degrid_f32": (C.c_int, [_VP, _VP, _VP, _VP, C.c_int32, _VP]),
     "gb_degrid_forward": (C.c_int, [_VP, _VP, _VP, _VP, _VP]),
     "gb_degrid_backward": (C.c_int, [_VP, _VP, _VP, _VP, _VP]),
+    "gb_grid_forward": (C.c_int, [_VP, _VP, _VP, _VP, _VP]),
+    "gb_grid_backward": (C.c_int, [_VP, _VP, _VP, _VP, _VP]),
+    "gb_grid_forward_f64": (C.c_int, [_VP, _VP, _VP, _VP, _VP]),
+    "gb_grid_backward_f64": (C.c_int, [_VP, _VP, _VP, _VP, _VP]),
+    "gb_degrid_forward_f64": (C.c_int, [_VP, _VP, _VP, _VP, _VP]),
+    "gb_degrid_backward_f64": (C.c_int, [_VP, _VP, _VP, _VP, _VP]),
     "gb_grid_f64": (C.c_int, [_VP, _VP, _VP, _VP, _VP]),
     "gb_degrid_f64": (C.c_int, [_VP, _VP, _VP, _VP, C.c_int32, _VP]),
     "gb_gcf_generate": (C.c_int, [C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_int32),
