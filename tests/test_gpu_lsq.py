@@ -165,7 +165,7 @@ def test_lsq_fifty_gradient_descent_iterations(lsq_setup):
     for it in range(50):
         r = forward_model(x * mask, t32, S["plan"], S["g32"]) - S["v"]
         L = torch.sum(r.real ** 2 + r.imag ** 2)
-        losses.append(float(L))
+        losses.append(float(L.detach()))
         x.grad = None
         L.backward()
         with torch.no_grad():
@@ -178,3 +178,42 @@ def test_lsq_fifty_gradient_descent_iterations(lsq_setup):
         e0 = float(torch.linalg.vector_norm(S["x_true"] * mask))
         e1 = float(torch.linalg.vector_norm((x - S["x_true"]) * mask))
     assert e1 < e0
+
+
+@pytest.mark.parametrize("prec", ["f64", "f32"])
+def test_lsq_grid_gradient_is_the_reference_gridder_on_the_residual(lsq_setup, prec):
+    """The gradient of L = ||D g - v||^2 with respect to the grid, as autograd
+    computes it (Degrid.backward: the hand-written gridding kernel on the
+    residual, 2 G r), against the reference's CPU gridder used as the adjoint:
+    the oracle's kern_scatter semantics (MS6/kernel/cpu/gridding/scatter.cpp:
+    89-111, grid += vis * gcf over every w-plane) applied to the same residual
+    r = D g - v, FP64.  FP64 within 1e-12, FP32 within 1e-5."""
+    import os
+
+    import torch
+
+    from oracle import oracle as O
+    from rc_gb300 import gcf as Gm
+    from rc_gb300.autograd import Degrid, ImageToGrid
+
+    S = lsq_setup
+    ob, n = S["ob"], S["n"]
+    rdt, cdt, gcf, tol = ((torch.float64, torch.complex128, S["g64"], 1e-12) if prec == "f64"
+                          else (torch.float32, torch.complex64, S["g32"], 1e-5))
+    with torch.no_grad():
+        g0 = ImageToGrid.apply((0.5 * S["x_true"]).to(rdt), S["t"].to(rdt))
+    g = g0.detach().clone().requires_grad_(True)
+    r = Degrid.apply(g, S["plan"], gcf) - S["v"].to(cdt)
+    L = torch.sum(r.real ** 2 + r.imag ** 2)
+    L.backward()
+    got = g.grad.detach().cpu().numpy().astype(np.complex128)
+
+    r_np = r.detach().cpu().numpy().astype(np.complex128)
+    offs, _ = Gm.layout(ob.supports)
+    plane = O.wbin(ob.uvw, ob.w_low, ob.w_high, len(ob.supports))
+    exp = np.zeros((n, n), np.complex128)
+    O.scatter_planes(ob.scale, n, int(ob.supports.max()), ob.uvw, r_np, plane, ob.supports,
+                     S["g64"].cpu().numpy(), offs, exp, nthreads=os.cpu_count() or 1)
+    exp *= 2.0
+    assert np.abs(exp).max() > 0
+    assert rel_l2(got, exp) < tol
