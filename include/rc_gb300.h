@@ -94,6 +94,16 @@ int nvGridder(double scale, int32_t grid_size, int32_t margin_size,
 /* Degridder type (MS6/programs/Kernel/Degrid.hs:146-147): vis_out = vis
  * minus sum(grid * gcf) for in-bound visibilities (no conjugate), u,v,w
  * copied; uvg is the full grid, min 0.
+ *
+ * Precision of both degridders: the products and sums run in double-float
+ * arithmetic on the FP32 pipe (each double split into two floats after a
+ * power-of-two scaling of its array), a 48-bit significand rather than FP64's
+ * 53: a sum errs by about 2^-48 of the sum of its terms' magnitudes (within
+ * 1e-12 relative of FP64 on every tested input).  Grid and GCF values below
+ * 2^-74 of their array's largest magnitude lose their low part, and those
+ * below 2^-126 of it count as zero.  Inputs holding an Inf, a NaN or a
+ * subnormal take a native FP64 loop instead.  The index math (pixel, phase,
+ * bounds) is FP64 and exact.
  * replaces MS6/kernel/gpu/gridding/kern_degrid_gpu1.cpp:61-81 */
 int kern_degrid_gpu1(double scale, int32_t grid_size, int32_t margin_size,
                      buffer_t *gcf, buffer_t *uvg, buffer_t *vis, buffer_t *vis_out);
@@ -213,8 +223,22 @@ int gb_grid_f32(gb_plan *plan, const float *d_vis, const float *d_gcf, float *d_
                 void *stream);
 int gb_degrid_f32(gb_plan *plan, const float *d_gcf, const float *d_grid, float *d_pred,
                   int32_t mode, void *stream);
-/* Forward / backward names of the pair: degrid forward = D, its backward
- * (vector-Jacobian product) = G; grid forward = G, backward = D. */
+/* Forward / backward names of the pair, for callers that differentiate
+ * through it (a least-squares imaging gradient; no counterpart in the
+ * reference, whose degridder is not an adjoint of its gridder).  Both
+ * operators are complex-linear, so a backward (vector-Jacobian product in the
+ * conjugate convention torch uses for complex tensors) is the adjoint:
+ *   gb_grid_forward:    grid += G vis                 (as gb_grid_f32)
+ *   gb_grid_backward:   vis_grad = G^H grid_grad = D grid_grad
+ *                       (as gb_degrid_f32 mode 0; overwrites vis_grad)
+ *   gb_degrid_forward:  pred = D grid                 (as gb_degrid_f32 mode 0)
+ *   gb_degrid_backward: grid_grad += D^H pred_grad = G pred_grad
+ *                       (as gb_grid_f32; accumulates into grid_grad)
+ * Arguments: plan, GCFs, the input, the output, stream. */
+int gb_grid_forward(gb_plan *plan, const float *d_gcf, const float *d_vis, float *d_grid,
+                    void *stream);
+int gb_grid_backward(gb_plan *plan, const float *d_gcf, const float *d_grid_grad,
+                     float *d_vis_grad, void *stream);
 int gb_degrid_forward(gb_plan *plan, const float *d_gcf, const float *d_grid,
                       float *d_pred, void *stream);
 int gb_degrid_backward(gb_plan *plan, const float *d_gcf, const float *d_pred_grad,
@@ -231,6 +255,16 @@ int gb_grid_f64(gb_plan *plan, const double *d_vis, const double *d_gcf, double 
                 void *stream);
 int gb_degrid_f64(gb_plan *plan, const double *d_gcf, const double *d_grid,
                   double *d_pred, int32_t mode, void *stream);
+/* The FP64 pair under the forward / backward names (meanings as for
+ * gb_grid_forward and the rest above). */
+int gb_grid_forward_f64(gb_plan *plan, const double *d_gcf, const double *d_vis,
+                        double *d_grid, void *stream);
+int gb_grid_backward_f64(gb_plan *plan, const double *d_gcf, const double *d_grid_grad,
+                         double *d_vis_grad, void *stream);
+int gb_degrid_forward_f64(gb_plan *plan, const double *d_gcf, const double *d_grid,
+                          double *d_pred, void *stream);
+int gb_degrid_backward_f64(gb_plan *plan, const double *d_gcf, const double *d_pred_grad,
+                           double *d_grid_grad, void *stream);
 
 /* On-GPU w-kernel generation (MS4/kernel/cpu/gcf/GCF.cpp semantics): for
  * each plane p, the FP64 phase screen exp(-2 pi i w_p (1 - sqrt(1-l^2-m^2)))
@@ -353,10 +387,13 @@ int gb_batch_degrid_f64(gb_batch *batch, const double *d_gcf, const double *cons
  * planes, n_vis * k^2 <= GB_NOALLOC_MAX_PIECES footprint pieces (k = pieces
  * per axis of the largest support, ceil(S / period_cap)), and at most
  * GB_NOALLOC_MAX_BINS (grid tile, thread-group class) bins; larger requests
- * return GB_ERR_CAPACITY before any GPU work.
+ * return GB_ERR_CAPACITY before any GPU work.  A grid more than 32767 tiles
+ * wide or high returns GB_ERR_ARG, as gb_plan_create does.
  *
  * The first call on a device looks up the array's device address
  * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * The address is kept for the process: after cudaDeviceReset on a device, do
+ * not call this entry point there again.
  * Every call on a device shares the array and leaves its contents behind; each
  * call clears what must start at zero.  Calls whose GPU work overlaps (other
  * streams, other host threads) race on the array: serialise them.  The call

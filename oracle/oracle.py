@@ -40,11 +40,22 @@ _f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
 _i32, _i64, _f64 = C.c_int32, C.c_int64, C.c_double
 
 
+def reference_root() -> str:
+    """The reference checkout the `ref` target compiles from: RC_REFERENCE in
+    the environment, else the Makefile's default."""
+    root = os.environ.get("RC_REFERENCE")
+    if root:
+        return root
+    r = subprocess.run(["make", "-s", "-C", HERE, "refroot"], capture_output=True, text=True)
+    return r.stdout.strip()
+
+
 def build(ref: bool = True) -> None:
     """Compile oracle/liboracle.so (and oracle/_ref when the reference is present)."""
     subprocess.run(["make", "-s", "-C", HERE, "liboracle.so"], check=True)
-    if ref and os.path.isdir("/root/reference/MS4"):
-        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+    root = reference_root() if ref else ""
+    if root and os.path.isdir(os.path.join(root, "MS4")):
+        subprocess.run(["make", "-s", "-C", HERE, "ref", "REFROOT=" + root], check=True)
 
 
 def lib():
