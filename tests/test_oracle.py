@@ -182,18 +182,31 @@ def test_gcf_phase_normalisation():
 
 
 # ---------------------------------------------------------------- reference MS4 binary
-def _coinciding_case(seed, G=128, S=8, nbl=23, ts=9):
+def _coinciding_case(seed, G=128, S=8, nbl=23, ts=9, edges=False, lattice=False):
     """Inputs where floor- and round-based conventions coincide: fractional
-    part in [k/8, k/8 + 1/16), k <= 3 (SURVEY of the two conventions)."""
+    part in [k/8, k/8 + 1/16), k <= 3 (the two conventions of MS4 and MS6).
+    edges: some footprints at the first and the last corner that MS6's
+    bounds rule keeps (x0 = 0 and x0 = G - S - 1, either axis).  lattice:
+    GCF values on a grid of 2^-10 (12 significant bits, so the fixtures that
+    store them compress; the products with the visibilities still round)."""
     rng = np.random.default_rng(seed)
     scale = 50.0
     pix = rng.integers(-G // 3, G // 3, size=(nbl, ts, 2)).astype(np.float64)
+    if edges:
+        lo, hi = S // 2 - G // 2, G // 2 - S // 2 - 1  # x0 = 0 and x0 = G - S - 1
+        corners = [(lo, lo), (hi, hi), (lo, hi), (hi, lo), (lo, 0), (0, hi)]
+        for c, (a, b) in enumerate(corners[:nbl * ts]):
+            pix[c % nbl, c // nbl] = (a, b)
     k = rng.integers(0, 4, size=(nbl, ts, 2))
     fr = k / 8 + rng.uniform(0, 1 / 16 - 1e-9, size=(nbl, ts, 2))
     uvw = np.zeros((nbl, ts, 3))
     uvw[..., :2] = (pix + fr) / scale
     vis = rng.standard_normal((nbl, ts)) + 1j * rng.standard_normal((nbl, ts))
-    gcf = rng.standard_normal((64, S, S)) + 1j * rng.standard_normal((64, S, S))
+    if lattice:
+        gcf = (rng.integers(-2048, 2049, (64, S, S)) +
+               1j * rng.integers(-2048, 2049, (64, S, S))) / 1024.0
+    else:
+        gcf = rng.standard_normal((64, S, S)) + 1j * rng.standard_normal((64, S, S))
     v5_ = np.zeros((nbl * ts, 5))
     v5_[:, :3] = uvw.reshape(-1, 3)
     v5_[:, 3] = vis.real.ravel()
@@ -227,9 +240,13 @@ def test_oracle_against_golden_fixtures():
         G = int(z[f"{tag}_G"])
         vis5, gcf = z[f"{tag}_vis5"], z[f"{tag}_gcf"]
         S = gcf.shape[-1]
+        ref = np.zeros(G * G, np.complex128)
+        ref[z[f"{tag}_gridnz"]] = z[f"{tag}_gridval"]
+        ref = ref.reshape(G, G)
         g = np.zeros((G, G), np.complex128)
         O.scatter(scale, G, S, vis5, gcf, g)
-        assert rel_l2(g, z[f"{tag}_grid"]) < 1e-14, tag
-        out = O.degrid(scale, G, S, gcf, z[f"{tag}_grid"], vis5)
+        assert np.array_equal(g != 0, ref != 0), tag
+        assert rel_l2(g, ref) < 1e-14, tag
+        out = O.degrid(scale, G, S, gcf, ref, vis5)
         pred = -((out[:, 3] - vis5[:, 3]) + 1j * (out[:, 4] - vis5[:, 4]))
         assert rel_l2(pred, z[f"{tag}_pred"]) < 1e-13, tag
