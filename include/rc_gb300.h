@@ -184,6 +184,16 @@ int gb_plan_stats(const gb_plan *plan, int64_t *stats7);
 #define GB_STAGE_ROWS 2
 int gb_plan_set_stage(gb_plan *plan, int32_t stage);
 
+/* 1 when the reference-ABI calls on the current device reach host buffers
+ * directly from their kernels (pageable memory through the host's page
+ * tables, e.g. Grace with NVLink-C2C): gridding and degridding then move only
+ * the 32 x 32-pixel grid blocks their visibilities touch, and kern_detile runs
+ * in place on the GPU.  0 when they copy
+ * whole buffers instead (no such access, or RC_GB300_HOST_DIRECT=0 in the
+ * environment when the first call was made); buffers not 16-byte aligned are
+ * always copied.  No counterpart in the reference. */
+int gb_host_direct(void);
+
 /* Test hook (host-side fault injection): let the next `after` device
  * allocations of the library succeed and fail the `count` after them with
  * GB_ERR_NOMEM, as a cudaMalloc out of memory would.  (0, 0) turns it off.

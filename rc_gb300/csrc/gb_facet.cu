@@ -183,6 +183,16 @@ extern "C" int kern_detile(buffer_t* in_grid, buffer_t* out_grid) {
   if (x1 <= x0 || y1 <= y0) return GB_OK;
   cudaStream_t s;
   if ((rc = stage_stream(&s))) return rc;
+  if (host_direct(in_grid->host, 2 * ip) && host_direct(out_grid->host, 2 * op)) {
+    // the GPU adds in place over the overlap, loads and stores over the link
+    k_detile<double2><<<blocks_of((int64_t)(x1 - x0) * (y1 - y0)), 256, 0, s>>>(
+        (const double2*)in_grid->host, ip, in_grid->min[1], in_grid->min[2],
+        (double2*)out_grid->host, op, out_grid->min[1], out_grid->min[2], x0, y0, x1 - x0,
+        y1 - y0);
+    GB_CUDA_TRY(cudaGetLastError());
+    GB_CUDA_TRY(cudaStreamSynchronize(s));
+    return GB_OK;
+  }
   void *d_in, *d_out;
   if ((rc = stage_buffer(0, (size_t)iw * ih * 16, &d_in)) ||
       (rc = stage_buffer(1, (size_t)ow * oh * 16, &d_out)))

@@ -11,9 +11,13 @@
 // are the reference's (MS6/kernel/cpu/gridding/scatter.cpp:56-111,
 // degrid.cpp:41-98) on Halide buffer_t host buffers.
 #include <stdio.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <algorithm>
+#include <mutex>
+#include <thread>
+#include <vector>
 
 #include "gb_common.cuh"
 #include "gb_plan.cuh"
@@ -253,19 +257,28 @@ __device__ __forceinline__ LaneIndex single_index(const double* __restrict__ vis
   return li;
 }
 
+// The record at visit position i: `order` (records by the grid block of their
+// footprint corner, so that neighbouring warps share grid lines in L2) or
+// index order.
+__device__ __forceinline__ int64_t visit_rec(const int32_t* __restrict__ order, int64_t i,
+                                             int64_t n) {
+  return order && i < n ? (int64_t)order[i] : i;
+}
+
 __global__ void k_scatter_single64(int64_t n, const double* __restrict__ vis5,
                                    const double2* __restrict__ gcf, double2* __restrict__ grid,
-                                   SingleGeo geo) {
+                                   SingleGeo geo, const int32_t* __restrict__ order) {
   const int lane = threadIdx.x & 31;
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
   for (int64_t t0 = 32 * (blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5)); t0 < n;
        t0 += 32 * warps) {
-    const LaneIndex mine = single_index(vis5, t0 + lane, n, geo);
+    const int64_t t = visit_rec(order, t0 + lane, n);
+    const LaneIndex mine = single_index(vis5, t, n, geo);
     const int m = (int)min((int64_t)32, n - t0);
     for (int j = 0; j < m; j++) {
       const LaneIndex ix = mine.from(j);
       if (!ix.keep) continue;
-      const double* r = vis5 + 5 * (t0 + j);
+      const double* r = vis5 + 5 * __shfl_sync(0xffffffffu, t, j);
       warp_scatter64(grid + (int64_t)ix.y0 * geo.pitch + ix.x0, geo.pitch,
                      gcf + (int64_t)ix.phase * geo.S * geo.S, geo.S, r[3], r[4], lane);
     }
@@ -281,14 +294,15 @@ __global__ void k_degrid_single64(int64_t n, const double* __restrict__ vis5,
                                   const float4* __restrict__ gcf_df,
                                   const float4* __restrict__ grid_df,
                                   const int* __restrict__ exps, double* __restrict__ out5,
-                                  SingleGeo geo) {
+                                  SingleGeo geo, const int32_t* __restrict__ order) {
   const int lane = threadIdx.x & 31;
   const bool df = exps[0] != kExpNonFinite && exps[1] != kExpNonFinite;
   const int kt = df_scale_exp(exps[0]) + df_scale_exp(exps[1]);
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
   for (int64_t t0 = 32 * (blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5)); t0 < n;
        t0 += 32 * warps) {
-    const int64_t t = t0 + lane;
+    const bool mine_ok = t0 + lane < n;
+    const int64_t t = visit_rec(order, t0 + lane, n);
     const LaneIndex mine = single_index(vis5, t, n, geo);
     const int m = (int)min((int64_t)32, n - t0);
     float4 acc_df = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -328,7 +342,7 @@ __global__ void k_degrid_single64(int64_t n, const double* __restrict__ vis5,
         if (lane == j) acc = a;
       }
     }
-    if (t < n) {
+    if (mine_ok) {
       if (df) acc = df_to_double(acc_df, kt);
       const double* r = vis5 + 5 * t;
       double* o = out5 + 5 * t;
@@ -356,19 +370,27 @@ __device__ __forceinline__ LaneIndex plane_index(const PlanDev& P, int64_t t) {
   return li;
 }
 
+// The visibility at visit position i: the plan's order (by the tile of the
+// footprint corner, so that a warp's and its neighbours' footprints share grid
+// lines in L2), or index order.
+__device__ __forceinline__ int64_t visit(const PlanDev& P, int64_t i) {
+  return P.order && i < P.n_vis ? (int64_t)P.order[i] : i;
+}
+
 __global__ void k_grid_plain64(PlanDev P, const double2* __restrict__ vis,
                                const double2* __restrict__ gcf, double2* __restrict__ grid) {
   const int lane = threadIdx.x & 31;
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
   for (int64_t t0 = 32 * (blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5));
        t0 < P.n_vis; t0 += 32 * warps) {
-    const LaneIndex mine = plane_index(P, t0 + lane);
+    const int64_t t = visit(P, t0 + lane);
+    const LaneIndex mine = plane_index(P, t);
     const int m = (int)min((int64_t)32, P.n_vis - t0);
     for (int j = 0; j < m; j++) {
       const LaneIndex ix = mine.from(j);
       if (!ix.keep) continue;
       const int32_t S = P.supports[ix.plane];
-      const double2 v = vis[t0 + j];
+      const double2 v = vis[__shfl_sync(0xffffffffu, t, j)];
       warp_scatter64(grid + (int64_t)ix.y0 * P.pitch + ix.x0, P.pitch,
                      gcf + P.gcf_offsets[ix.plane] + (int64_t)ix.phase * S * S, S, v.x, v.y,
                      lane);
@@ -390,7 +412,8 @@ __global__ void k_degrid_plain64(PlanDev P, const double2* __restrict__ gcf,
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
   for (int64_t t0 = 32 * (blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5));
        t0 < P.n_vis; t0 += 32 * warps) {
-    const int64_t t = t0 + lane;
+    const bool mine_ok = t0 + lane < P.n_vis;
+    const int64_t t = visit(P, t0 + lane);
     const LaneIndex mine = plane_index(P, t);
     const int m = (int)min((int64_t)32, P.n_vis - t0);
     float4 acc_df = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -411,7 +434,7 @@ __global__ void k_degrid_plain64(PlanDev P, const double2* __restrict__ gcf,
         if (lane == j) acc = a;
       }
     }
-    if (t < P.n_vis) {
+    if (mine_ok) {
       if (df) acc = df_to_double(acc_df, kt);
       if (mode == 1) {
         acc.x = -acc.x;
@@ -439,6 +462,170 @@ __global__ void k_add_c128(double2* __restrict__ a, const double2* __restrict__ 
     const double2 x = a[i], y = b[i];
     a[i] = make_double2(x.x + y.x, x.y + y.y);
   }
+}
+
+// ---------------------------------------------------------------- host-direct staging
+// On a GPU that reaches pageable host memory through the host's own page
+// tables (Grace with NVLink-C2C: cudaDevAttrPageableMemoryAccess and
+// cudaDevAttrPageableMemoryAccessUsesHostPageTables), the synchronous ABI
+// calls move only the grid blocks their visibilities touch instead of the
+// whole grid: a mark kernel flags every kBlk x kBlk block that a kept
+// footprint overlaps (the same index math and bounds rule as the gridder, so
+// no kept tap falls outside a marked block); gridding accumulates into a
+// device buffer zeroed on the marked blocks, and a flush kernel adds those
+// blocks into the caller's grid in place, with loads and stores over the link;
+// degridding gathers the marked blocks of the caller's grid into a device
+// buffer whose other blocks are zeroed.  The kernels touch the caller's
+// buffer only inside the region its buffer_t describes (rows of W complex
+// elements, `row` doubles apart).  Elsewhere, for a host buffer that is not
+// 16-byte aligned, or with RC_GB300_HOST_DIRECT=0 in the environment, the
+// whole grid is copied as before (host_direct, gb_runtime.cu).
+constexpr int kBlk = 32;
+
+// marks[by * nbx + bx] = 1 for every block a kept footprint overlaps
+__global__ void k_mark_blocks(int64_t n, const double* __restrict__ vis5, SingleGeo geo, int nbx,
+                              unsigned char* __restrict__ marks) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const VisIndex ix = vis_index(vis5[5 * t], vis5[5 * t + 1], geo.scale, geo.grid_size, geo.S,
+                                  geo.margin, geo.min_x, geo.min_y, geo.ext_x, geo.ext_y);
+    if (!ix.keep) continue;
+    const int x0 = ix.x0 - geo.min_x, y0 = ix.y0 - geo.min_y;
+    const int bx1 = (x0 + geo.S - 1) / kBlk, by1 = (y0 + geo.S - 1) / kBlk;
+    for (int by = y0 / kBlk; by <= by1; by++)
+      for (int bx = x0 / kBlk; bx <= bx1; bx++) marks[by * nbx + bx] = 1;
+  }
+}
+
+// One CTA per block of a W x H complex128 region (device rows W apart):
+// zero the marked blocks.
+__global__ void k_zero_marked(double2* __restrict__ d, int W, int H, int nbx,
+                              const unsigned char* __restrict__ marks) {
+  const int b = blockIdx.x;
+  if (!marks[b]) return;
+  const int bx = b % nbx, by = b / nbx;
+  for (int k = threadIdx.x; k < kBlk * kBlk; k += blockDim.x) {
+    const int x = bx * kBlk + (k % kBlk), y = by * kBlk + k / kBlk;
+    if (x < W && y < H) d[(int64_t)y * W + x] = make_double2(0.0, 0.0);
+  }
+}
+
+// host grid (rows `row` doubles apart) += d over the marked blocks
+__global__ void k_flush_host(double* __restrict__ host, int64_t row,
+                             const double2* __restrict__ d, int W, int H, int nbx,
+                             const unsigned char* __restrict__ marks) {
+  const int b = blockIdx.x;
+  if (!marks[b]) return;
+  const int bx = b % nbx, by = b / nbx;
+  for (int k = threadIdx.x; k < kBlk * kBlk; k += blockDim.x) {
+    const int x = bx * kBlk + (k % kBlk), y = by * kBlk + k / kBlk;
+    if (x < W && y < H) {
+      double2* hp = reinterpret_cast<double2*>(host + (int64_t)y * row) + x;
+      const double2 a = *hp, v = d[(int64_t)y * W + x];
+      *hp = make_double2(a.x + v.x, a.y + v.y);
+    }
+  }
+}
+
+// d = the host grid on the marked blocks, 0 on the others (every block written)
+__global__ void k_gather_host(double2* __restrict__ d, const double* __restrict__ host,
+                              int64_t row, int W, int H, int nbx,
+                              const unsigned char* __restrict__ marks) {
+  const int b = blockIdx.x;
+  const bool on = marks[b] != 0;
+  const int bx = b % nbx, by = b / nbx;
+  for (int k = threadIdx.x; k < kBlk * kBlk; k += blockDim.x) {
+    const int x = bx * kBlk + (k % kBlk), y = by * kBlk + k / kBlk;
+    if (x < W && y < H)
+      d[(int64_t)y * W + x] =
+          on ? *(reinterpret_cast<const double2*>(host + (int64_t)y * row) + x)
+             : make_double2(0.0, 0.0);
+  }
+}
+
+// Marks of the kept footprints of n device records over a W x H region.
+static int mark_blocks(int64_t n, const void* d_vis, const SingleGeo& geo, int nbx, int nby,
+                       unsigned char* marks, cudaStream_t s) {
+  GB_CUDA_TRY(cudaMemsetAsync(marks, 0, (size_t)nbx * nby, s));
+  const int blocks = (int)std::clamp<int64_t>((n + 255) / 256, 1, (int64_t)sm_count() * 8);
+  k_mark_blocks<<<blocks, 256, 0, s>>>(n, (const double*)d_vis, geo, nbx, marks);
+  GB_CUDA_TRY(cudaGetLastError());
+  return GB_OK;
+}
+
+// Counting sort of a call's records by the kBlk x kBlk block of their
+// footprint corner (kept records; the others last), on the device: a
+// histogram, a one-block exclusive scan, a scatter of record indices.
+__device__ __forceinline__ int block_key(const double* __restrict__ vis5, int64_t t,
+                                         const SingleGeo& geo, int nbx, int nkeys) {
+  const VisIndex ix = vis_index(vis5[5 * t], vis5[5 * t + 1], geo.scale, geo.grid_size, geo.S,
+                                geo.margin, geo.min_x, geo.min_y, geo.ext_x, geo.ext_y);
+  return ix.keep ? ((ix.y0 - geo.min_y) / kBlk) * nbx + (ix.x0 - geo.min_x) / kBlk : nkeys - 1;
+}
+
+__global__ void k_key_hist(int64_t n, const double* __restrict__ vis5, SingleGeo geo, int nbx,
+                           int nkeys, int32_t* __restrict__ hist) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
+       t += (int64_t)gridDim.x * blockDim.x)
+    atomicAdd(&hist[block_key(vis5, t, geo, nbx, nkeys)], 1);
+}
+
+// offs = exclusive scan of hist over nkeys entries (one block of 1024 threads)
+__global__ void __launch_bounds__(1024) k_scan_keys(const int32_t* __restrict__ hist,
+                                                    int32_t* __restrict__ offs, int nkeys) {
+  __shared__ int32_t part[1024];
+  const int tid = threadIdx.x, chunk = (nkeys + 1023) / 1024;
+  const int k0 = min(nkeys, tid * chunk), k1 = min(nkeys, k0 + chunk);
+  int32_t sum = 0;
+  for (int k = k0; k < k1; k++) sum += hist[k];
+  part[tid] = sum;
+  __syncthreads();
+  for (int off = 1; off < 1024; off <<= 1) {
+    const int32_t a = tid >= off ? part[tid - off] : 0;
+    __syncthreads();
+    part[tid] += a;
+    __syncthreads();
+  }
+  int32_t pre = part[tid] - sum;
+  for (int k = k0; k < k1; k++) {
+    offs[k] = pre;
+    pre += hist[k];
+  }
+}
+
+__global__ void k_key_scatter(int64_t n, const double* __restrict__ vis5, SingleGeo geo, int nbx,
+                              int nkeys, const int32_t* __restrict__ offs,
+                              int32_t* __restrict__ cursor, int32_t* __restrict__ order) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int k = block_key(vis5, t, geo, nbx, nkeys);
+    order[offs[k] + atomicAdd(&cursor[k], 1)] = (int32_t)t;
+  }
+}
+
+// The visit order of n device records (staging slots 7 and 8).
+static int order_by_block(int64_t n, const void* d_vis, const SingleGeo& geo, int32_t** order,
+                          cudaStream_t s) {
+  const int nbx = (geo.ext_x + kBlk - 1) / kBlk, nby = (geo.ext_y + kBlk - 1) / kBlk;
+  const int nkeys = nbx * nby + 1;
+  void *d_keys, *d_order;
+  int rc;
+  if ((rc = stage_buffer(7, (size_t)3 * nkeys * sizeof(int32_t), &d_keys)) ||
+      (rc = stage_buffer(8, (size_t)n * sizeof(int32_t), &d_order)))
+    return rc;
+  int32_t* hist = (int32_t*)d_keys;
+  int32_t* offs = hist + nkeys;
+  int32_t* cursor = offs + nkeys;
+  GB_CUDA_TRY(cudaMemsetAsync(hist, 0, sizeof(int32_t) * nkeys, s));
+  GB_CUDA_TRY(cudaMemsetAsync(cursor, 0, sizeof(int32_t) * nkeys, s));
+  const int blocks = (int)std::clamp<int64_t>((n + 255) / 256, 1, (int64_t)sm_count() * 8);
+  const double* v = (const double*)d_vis;
+  k_key_hist<<<blocks, 256, 0, s>>>(n, v, geo, nbx, nkeys, hist);
+  k_scan_keys<<<1, 1024, 0, s>>>(hist, offs, nkeys);
+  k_key_scatter<<<blocks, 256, 0, s>>>(n, v, geo, nbx, nkeys, offs, cursor, (int32_t*)d_order);
+  GB_CUDA_TRY(cudaGetLastError());
+  *order = (int32_t*)d_order;
+  return GB_OK;
 }
 
 // Exponents and double-float splits of a grid region (ext_y rows of ext_x
@@ -600,6 +787,36 @@ static int compat_scatter(const char* who, int size_err, double scale, int32_t g
   const int32_t W = uvg->extent[1], H = uvg->extent[2];
   const int64_t row = grid_row_doubles(uvg);
   if (n == 0) return GB_OK;  // the grid is unchanged
+  if (host_direct(uvg->host, row)) {
+    cudaStream_t s;
+    if ((rc = stage_stream(&s))) return rc;
+    void *d_vis, *d_gcf, *d_acc, *d_marks;
+    const size_t gcf_bytes = (size_t)GB_PHASES * S * S * 16;
+    const int nbx = (W + kBlk - 1) / kBlk, nby = (H + kBlk - 1) / kBlk;
+    if ((rc = stage_buffer(0, (size_t)n * 40, &d_vis)) ||
+        (rc = stage_buffer(1, gcf_bytes, &d_gcf)) ||
+        (rc = stage_buffer(4, (size_t)W * H * 16, &d_acc)) ||
+        (rc = stage_buffer(6, (size_t)nbx * nby, &d_marks)))
+      return rc;
+    GB_CUDA_TRY(cudaMemcpyAsync(d_vis, vis->host, (size_t)n * 40, cudaMemcpyHostToDevice, s));
+    GB_CUDA_TRY(cudaMemcpyAsync(d_gcf, gcf->host, gcf_bytes, cudaMemcpyHostToDevice, s));
+    SingleGeo geo{scale, grid_size, margin, S, uvg->min[1], uvg->min[2], W, H, (int64_t)W};
+    unsigned char* marks = (unsigned char*)d_marks;
+    int32_t* order = nullptr;
+    if ((rc = mark_blocks(n, d_vis, geo, nbx, nby, marks, s)) ||
+        (rc = order_by_block(n, d_vis, geo, &order, s)))
+      return rc;
+    k_zero_marked<<<nbx * nby, 256, 0, s>>>((double2*)d_acc, W, H, nbx, marks);
+    int blocks;
+    const int threads = plain_grid_dims(n, &blocks);
+    k_scatter_single64<<<blocks, threads, 0, s>>>(n, (const double*)d_vis, (const double2*)d_gcf,
+                                                  (double2*)d_acc, geo, order);
+    k_flush_host<<<nbx * nby, 256, 0, s>>>((double*)uvg->host, row, (const double2*)d_acc, W, H,
+                                           nbx, marks);
+    GB_CUDA_TRY(cudaGetLastError());
+    GB_CUDA_TRY(cudaStreamSynchronize(s));
+    return GB_OK;
+  }
   cudaStream_t s, s2;
   cudaEvent_t* evs;
   if ((rc = stage_stream(&s)) || (rc = stage_aux(&s2, &evs))) return rc;
@@ -622,7 +839,7 @@ static int compat_scatter(const char* who, int size_err, double scale, int32_t g
   int blocks;
   const int threads = plain_grid_dims(n, &blocks);
   k_scatter_single64<<<blocks, threads, 0, s2>>>(n, (const double*)d_vis, (const double2*)d_gcf,
-                                                 (double2*)d_acc, geo);
+                                                 (double2*)d_acc, geo, nullptr);
   GB_TRY_DRAIN(cudaGetLastError(), s, s2);
   GB_TRY_DRAIN(cudaEventRecord(ev, s2), s, s2);
   GB_TRY_DRAIN(cudaMemcpy2DAsync(d_grid, (size_t)W * 16, uvg->host, (size_t)row * 8,
@@ -681,13 +898,41 @@ static int compat_degrid(const char* who, int size_err, double scale, int32_t gr
   GB_CUDA_TRY(cudaMemcpyAsync(d_vis, (const double*)vis->host + 5 * first, (size_t)n * 40,
                               cudaMemcpyHostToDevice, s));
   GB_CUDA_TRY(cudaMemcpyAsync(d_gcf, gcf->host, gcf_bytes, cudaMemcpyHostToDevice, s));
-  GB_CUDA_TRY(cudaMemcpy2DAsync(d_grid, (size_t)W * 16, uvg->host, (size_t)row * 8, (size_t)W * 16,
-                                H, cudaMemcpyHostToDevice, s));
   SingleGeo geo{scale, grid_size, margin, S, uvg->min[1], uvg->min[2], W, H, (int64_t)W};
+  const bool direct = host_direct(uvg->host, row);
+  if (direct) {
+    // only the blocks the visibilities read, straight from the caller's grid
+    void* d_marks;
+    const int nbx = (W + kBlk - 1) / kBlk, nby = (H + kBlk - 1) / kBlk;
+    if ((rc = stage_buffer(6, (size_t)nbx * nby, &d_marks))) return rc;
+    unsigned char* marks = (unsigned char*)d_marks;
+    if ((rc = mark_blocks(n, d_vis, geo, nbx, nby, marks, s))) return rc;
+    k_gather_host<<<nbx * nby, 256, 0, s>>>((double2*)d_grid, (const double*)uvg->host, row, W, H,
+                                            nbx, marks);
+    GB_CUDA_TRY(cudaGetLastError());
+  } else {
+    GB_CUDA_TRY(cudaMemcpy2DAsync(d_grid, (size_t)W * 16, uvg->host, (size_t)row * 8,
+                                  (size_t)W * 16, H, cudaMemcpyHostToDevice, s));
+  }
   if ((rc = df_prepare((const double*)d_grid, W, H, W, (const double*)d_gcf,
                        (int64_t)GB_PHASES * S * S, (float4*)d_grid_df, (float4*)d_gcf_df, d_exps,
                        s)))
     return rc;
+  if (direct) {
+    // one launch over the records in grid-block order (neighbouring warps
+    // gather from the same grid lines), then one download of the results
+    int32_t* order = nullptr;
+    if ((rc = order_by_block(n, d_vis, geo, &order, s))) return rc;
+    int blocks;
+    const int threads = plain_grid_dims(n, &blocks);
+    k_degrid_single64<<<blocks, threads, 0, s>>>(
+        n, (const double*)d_vis, (const double2*)d_gcf, (const double2*)d_grid,
+        (const float4*)d_gcf_df, (const float4*)d_grid_df, d_exps, (double*)d_out, geo, order);
+    GB_CUDA_TRY(cudaGetLastError());
+    GB_CUDA_TRY(cudaMemcpyAsync(vis_out->host, d_out, (size_t)n * 40, cudaMemcpyDeviceToHost, s));
+    GB_CUDA_TRY(cudaStreamSynchronize(s));
+    return GB_OK;
+  }
   // In chunks of visibilities: every chunk's kernel is queued first, each
   // followed by its event; a chunk's results then go down on the second stream
   // while the later chunks are degridded.  (A copy into pageable memory returns
@@ -703,7 +948,8 @@ static int compat_degrid(const char* who, int size_err, double scale, int32_t gr
     const int threads = plain_grid_dims(c1 - c0, &blocks);
     k_degrid_single64<<<blocks, threads, 0, s>>>(
         c1 - c0, (const double*)d_vis + 5 * c0, (const double2*)d_gcf, (const double2*)d_grid,
-        (const float4*)d_gcf_df, (const float4*)d_grid_df, d_exps, (double*)d_out + 5 * c0, geo);
+        (const float4*)d_gcf_df, (const float4*)d_grid_df, d_exps, (double*)d_out + 5 * c0, geo,
+        nullptr);
     GB_TRY_DRAIN(cudaGetLastError(), s, s2);
     GB_TRY_DRAIN(cudaEventRecord(evs[c], s), s, s2);
   }
@@ -770,7 +1016,8 @@ extern "C" int kern_degrid(double scale, int32_t grid_size, int32_t margin_size,
 
 // kern_init (init.cpp:8-15): zero the complex grid region described by uvg.
 // The buffer is host memory and the reference's result is wanted there, so
-// this is a host memset of the region (no device round trip).
+// this is a host memset of the region (no device round trip), on up to eight
+// host threads for a large grid.
 extern "C" int kern_init(buffer_t* uvg) {
   if (!uvg) {
     gb_set_error(GB_ERR_ARG, "kern_init: NULL buffer");
@@ -780,8 +1027,31 @@ extern "C" int kern_init(buffer_t* uvg) {
   if (rc) return rc;
   const int64_t row = grid_row_doubles(uvg);
   double* p = (double*)uvg->host;
-  for (int32_t y = 0; y < uvg->extent[2]; y++)
-    memset(p + (int64_t)y * row, 0, (size_t)uvg->extent[1] * 16);
+  // A large grid is zeroed by several host threads, rows split between them:
+  // zeroing is also the first touch of a freshly allocated buffer, so it stays
+  // on the host (a GPU touching pages first through the host page tables pays
+  // a fault per page).
+  const int32_t H = uvg->extent[2];
+  const size_t rowb = (size_t)uvg->extent[1] * 16;
+  const int nt = (int)std::min<int64_t>(8, (int64_t)H * rowb >> 24);  // one per 16 MB
+  auto zero_rows = [p, row, rowb](int32_t y0, int32_t y1) {
+    for (int32_t y = y0; y < y1; y++) memset(p + (int64_t)y * row, 0, rowb);
+  };
+  if (nt < 2) {
+    zero_rows(0, H);
+    return GB_OK;
+  }
+  std::vector<std::thread> ts;
+  for (int k = 1; k < nt; k++) {
+    const int32_t y0 = (int32_t)((int64_t)H * k / nt), y1 = (int32_t)((int64_t)H * (k + 1) / nt);
+    try {
+      ts.emplace_back(zero_rows, y0, y1);
+    } catch (...) {  // no thread to be had: this one does those rows too
+      zero_rows(y0, y1);
+    }
+  }
+  zero_rows(0, (int32_t)((int64_t)H / nt));
+  for (auto& t : ts) t.join();
   return GB_OK;
 }
 

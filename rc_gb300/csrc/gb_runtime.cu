@@ -1,6 +1,7 @@
 // Library-wide runtime pieces: per-thread error string, version, the
 // per-thread device staging pool used by the reference-ABI entry points, and
 // small device utilities.
+#include <stdlib.h>
 #include <stdarg.h>
 #include <stdio.h>
 #include <string.h>
@@ -161,6 +162,26 @@ int sm_count() {
   return cached;
 }
 
+static bool host_direct_device() {
+  static int cached[64];
+  static std::once_flag once[64];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return false;
+  std::call_once(once[dev], [dev] {
+    int pma = 0, pmh = 0;
+    cudaDeviceGetAttribute(&pma, cudaDevAttrPageableMemoryAccess, dev);
+    cudaDeviceGetAttribute(&pmh, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev);
+    const char* env = getenv("RC_GB300_HOST_DIRECT");
+    cached[dev] = pma == 1 && pmh == 1 && !(env && env[0] == '0');
+  });
+  return cached[dev] != 0;
+}
+
+bool host_direct(const void* host, int64_t row_doubles) {
+  return host && (reinterpret_cast<uintptr_t>(host) & 15) == 0 && (row_doubles & 1) == 0 &&
+         host_direct_device();
+}
+
 }  // namespace gb
 
 extern "C" int gb_grid_zero_f32(float* d_grid, int64_t n_complex, void* stream) {
@@ -172,6 +193,8 @@ extern "C" int gb_grid_zero_f32(float* d_grid, int64_t n_complex, void* stream) 
   GB_CUDA_TRY(cudaMemsetAsync(d_grid, 0, (size_t)n_complex * 8, (cudaStream_t)stream));
   return GB_OK;
 }
+
+extern "C" int gb_host_direct(void) { return gb::host_direct_device() ? 1 : 0; }
 
 extern "C" int gb_debug_fail_allocs(int32_t after, int32_t count) {
   if (after < 0 || count < 0) {

@@ -3,10 +3,11 @@
 
 #include <cuda_runtime.h>
 #include <stddef.h>
+#include <stdint.h>
 
 namespace gb {
 
-constexpr int kStageSlots = 6;
+constexpr int kStageSlots = 9;
 constexpr int kAuxEvents = 4;
 
 // Per-host-thread stream and grow-only device buffers used by the synchronous
@@ -18,6 +19,13 @@ int stage_buffer(int slot, size_t bytes, void** out);
 int stage_aux(cudaStream_t* s2, cudaEvent_t** ev);
 
 int sm_count();
+
+// True when kernels on the current device may read and write this pageable
+// host buffer directly (through the host's page tables, NVLink-C2C on Grace):
+// the device reports pageable memory access using host page tables, the
+// pointer is 16-byte aligned, the row pitch is an even number of doubles, and
+// RC_GB300_HOST_DIRECT is not "0".
+bool host_direct(const void* host, int64_t row_doubles);
 
 // Every device allocation of the library goes through here: cudaMalloc, or
 // GB_ERR_NOMEM when the allocation-failure hook (gb_debug_fail_allocs) says so.

@@ -133,6 +133,7 @@ SIGNATURES = {
     "gb_plan_device_status": (C.c_int, [_VP, C.POINTER(C.c_int32), _VP]),
     "gb_plan_set_stage": (C.c_int, [_VP, C.c_int32]),
     "gb_debug_fail_allocs": (C.c_int, [C.c_int32, C.c_int32]),
+    "gb_host_direct": (C.c_int, []),
     "gb_checked_violations": (C.c_int, [C.POINTER(C.c_int64)]),
     "gb_checked_selftest": (C.c_int, []),
     "kern_fft": (C.c_int, [_VP, _VP]),

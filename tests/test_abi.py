@@ -112,3 +112,18 @@ def test_empty_calls_need_no_gpu():
     # the size codes still come first
     assert compat.call_scatter("kern_scatter_gpu1", 1.0, 16, 8, vis5,
                                np.ones((64, 12, 12), np.complex128), grid) == -222
+
+
+def test_kern_init_zeroes_a_large_grid_on_host_threads():
+    """kern_init (MS6/kernel/cpu/gridding/init.cpp:8-15) is host work: a 64 MB
+    grid with a row pitch wider than its rows is zeroed (rows split between
+    host threads) and the columns past the rows stay as they were."""
+    import numpy as np
+
+    from rc_gb300 import compat
+
+    L = lib.load()
+    big = np.full((4096, 1024), 3 + 4j)
+    b = compat.buf(big.view(np.float64), [(2, 1), (1000, 2), (4096, 2048)], (0, 0, 0, 0))
+    assert L.kern_init(C.byref(b)) == 0
+    assert (big[:, :1000] == 0).all() and (big[:, 1000:] == 3 + 4j).all()
