@@ -29,7 +29,9 @@
 #include <cmath>
 #include <cstdio>
 #include <stdexcept>
+#include <memory>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "rc_gb300.h"
@@ -125,10 +127,33 @@ struct VisBin {
   Vis vis;
 };
 
+namespace detail {
+// An allocator whose value-initialisation leaves doubles uninitialised: grid
+// buffers are allocated like Flow's (posix_memalign, Flow/Vector.hs:173-190)
+// and zeroed once, by kern_init, not twice.
+template <class T>
+struct NoInit : std::allocator<T> {
+  template <class U>
+  struct rebind {
+    using other = NoInit<U>;
+  };
+  NoInit() = default;
+  template <class U>
+  NoInit(const NoInit<U>&) {}
+  template <class U, class... A>
+  void construct(U* p, A&&... a) {
+    if constexpr (sizeof...(A) == 0)
+      ::new ((void*)p) U;
+    else
+      ::new ((void*)p) U(std::forward<A>(a)...);
+  }
+};
+}  // namespace detail
+
 // A complex grid region: dims (2, width, height), strides (1, 2, 2 width),
 // mins (0, min_u, min_v) (Data.hs:64-76, 93-97).
 struct UVGrid {
-  std::vector<double> data;
+  std::vector<double, detail::NoInit<double>> data;
   int min_u = 0, min_v = 0, width = 0, height = 0;
 };
 
@@ -174,13 +199,19 @@ inline buffer_t uvg_buffer(UVGrid& g) {
 inline buffer_t image_buffer(Image& im) {
   return make_buffer(im.data.data(), {im.width, im.height}, {1, im.width}, {0, 0});
 }
-inline UVGrid zero_grid(int min_u, int min_v, int width, int height) {
+// A grid region whose values the caller zeroes (kern_init) or overwrites.
+inline UVGrid alloc_grid(int min_u, int min_v, int width, int height) {
   UVGrid g;
   g.min_u = min_u;
   g.min_v = min_v;
   g.width = width;
   g.height = height;
-  g.data.assign((size_t)2 * width * height, 0.0);
+  g.data.resize((size_t)2 * width * height);
+  return g;
+}
+inline UVGrid zero_grid(int min_u, int min_v, int width, int height) {
+  UVGrid g = alloc_grid(min_u, min_v, width, height);
+  std::fill(g.data.begin(), g.data.end(), 0.0);
   return g;
 }
 }  // namespace detail
@@ -229,12 +260,24 @@ inline std::vector<VisBin> binner(const GridPar& gp, const Vis& vis, Range u, Ra
   const double vl = gridXY2UV(gp, v.low), vh = gridXY2UV(gp, v.high);
   std::vector<VisBin> out(bins.size());
   for (size_t b = 0; b < bins.size(); b++) out[b].bin = bins[b];
+  // binSizer's lows never decrease: lookupLE is then a binary search (the last
+  // low <= w is the last of equal lows too)
+  std::vector<double> lows(bins.size());
+  bool sorted = true;
+  for (size_t b = 0; b < bins.size(); b++) {
+    lows[b] = bins[b].low;
+    sorted = sorted && (b == 0 || !(lows[b] < lows[b - 1])) && lows[b] == lows[b];
+  }
   for (int64_t i = 0; i < vis.size(); i++) {
     const double* r = &vis.rec[5 * i];
     if (!(ul <= r[0] && r[0] < uh && vl <= r[1] && r[1] < vh)) continue;
     int k = -1;  // Map.lookupLE over the bins' lows (the last of equal lows)
-    for (size_t b = 0; b < bins.size(); b++)
-      if (bins[b].low <= r[2] && (k < 0 || bins[b].low >= bins[k].low)) k = (int)b;
+    if (sorted) {
+      k = (int)(std::upper_bound(lows.begin(), lows.end(), r[2]) - lows.begin()) - 1;
+    } else {
+      for (size_t b = 0; b < bins.size(); b++)
+        if (bins[b].low <= r[2] && (k < 0 || bins[b].low >= bins[k].low)) k = (int)b;
+    }
     if (k < 0 || !(r[2] < bins[k].high)) continue;
     out[k].vis.rec.insert(out[k].vis.rec.end(), r, r + 5);
   }
@@ -344,7 +387,7 @@ inline Vis oskarReader(const TaskData& td, int freq, int pol, int64_t low, int64
 // every side (Data.hs:71-76), zeroed by kern_init.
 inline UVGrid gridInit(const GCFPar& gcfp, Range u, Range v) {
   const int m = gcfMaxSize(gcfp) / 2;
-  UVGrid g = detail::zero_grid(u.low - m, v.low - m, u.size() + 2 * m, v.size() + 2 * m);
+  UVGrid g = detail::alloc_grid(u.low - m, v.low - m, u.size() + 2 * m, v.size() + 2 * m);
   buffer_t b = detail::uvg_buffer(g);
   check(kern_init(&b), "gridInit");
   return g;
@@ -377,7 +420,7 @@ inline void gridKernel(GridKernelType kt, const GridPar& gp, const GCFPar& gcfp,
 
 // gridInitDetile (Gridder.hs:76-77): the full grid without margins, zeroed.
 inline UVGrid gridInitDetile(Range u, Range v) {
-  UVGrid g = detail::zero_grid(u.low, v.low, u.size(), v.size());
+  UVGrid g = detail::alloc_grid(u.low, v.low, u.size(), v.size());
   buffer_t b = detail::uvg_buffer(g);
   check(kern_init(&b), "gridInitDetile");
   return g;

@@ -213,6 +213,43 @@ def tile_bins(vis5, height, scale, u_range, v_range, bins):
     return out
 
 
+def tile_bins_vec(vis5, height, scale, u_range, v_range, bins):
+    """tile_bins for finite w, vectorised (the same arithmetic in the same
+    order, so the same bins, counts and records): the lows are non-decreasing,
+    so Map.lookupLE (the last bin whose low <= w, the last of equal lows) is a
+    right-sided binary search."""
+    vis5 = np.asarray(vis5, np.float64)
+    u, v, w = vis5[:, 0], vis5[:, 1], vis5[:, 2]
+    umin, umax = xy2uv(height, scale, u_range[0]), xy2uv(height, scale, u_range[1])
+    vmin, vmax = xy2uv(height, scale, v_range[0]), xy2uv(height, scale, v_range[1])
+    inside = (u >= umin) & (u < umax) & (v >= vmin) & (v < vmax)
+    wi = w[inside]
+    assert np.isfinite(wi).all(), "tile_bins_vec: finite w only (tile_bins handles the rest)"
+    low = min(0.0, float(wi.min())) if len(wi) else 0.0
+    high0 = max(0.0, float(wi.max())) if len(wi) else 0.0
+    high = high0 + (high0 - low) * 0.0001
+    starts = [low + b * (high - low) / bins for b in range(bins + 1)]
+    ok = (wi >= low) & (wi <= high)
+    if high > low:
+        f = np.floor((wi[ok] - low) / (high - low) * bins)
+    else:
+        f = np.zeros(int(ok.sum()))
+    counts = np.bincount(np.clip(f, 0, bins - 1).astype(np.int64), minlength=bins)
+    idx = np.flatnonzero(inside)
+    k = np.searchsorted(np.asarray(starts[:bins]), wi, side="right") - 1
+    keep = k >= 0
+    kk = np.where(keep, k, 0)
+    keep &= wi < np.asarray(starts)[kk + 1]
+    out = []
+    for b in range(bins):
+        r = vis5[idx[keep & (k == b)]]
+        c = int(counts[b])
+        if len(r) < c:
+            r = np.vstack([r, np.zeros((c - len(r), 5))])
+        out.append((starts[b], starts[b + 1], c, r))
+    return out
+
+
 # ---------------------------------------------------------------- GCF generation (MS4 spec)
 def gcf_layers(w, support, max_support, t2, taper=None, over=OVER):
     """One w-plane's oversampled GCF in the MS6 layout [ou + 8*ov][sy][sx] (complex128).

@@ -104,6 +104,33 @@ def build(force: bool = False, ptxas_verbose: bool = False, verbose: bool = Fals
     return lib_out
 
 
+STRATEGY_SRC = os.path.join(HERE, "host", "gridding_strategy.cpp")
+
+
+def strategy_program(out_dir: str | None = None, ms5: bool = False) -> str:
+    """Compile host/gridding_strategy.cpp (the MS6 gridding strategy on the C++
+    host layer, include/rc_kernels.hpp) against librc_gb300.so (or, ms5=True,
+    librc_gb300_ms5.so with -DGB_MS5_ABI); returns the executable's path.
+    Rebuilt when older than its sources or the library."""
+    lib_out = build(ms5=ms5)
+    out_dir = out_dir or BUILD
+    os.makedirs(out_dir, exist_ok=True)
+    exe = os.path.join(out_dir, "gridding_strategy_ms5" if ms5 else "gridding_strategy")
+    deps = [STRATEGY_SRC, lib_out] + glob.glob(os.path.join(INCLUDE, "*"))
+    if os.path.exists(exe) and all(os.path.getmtime(d) <= os.path.getmtime(exe) for d in deps):
+        return exe
+    cmd = [os.environ.get("CXX", "g++"), "-std=c++17", "-O2", "-Wall", "-Wextra", "-pthread",
+           "-I", INCLUDE, STRATEGY_SRC, "-L", HERE,
+           "-lrc_gb300_ms5" if ms5 else "-lrc_gb300", "-Wl,-rpath," + HERE, "-o", exe + ".tmp"]
+    if ms5:
+        cmd.insert(1, "-DGB_MS5_ABI")
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0 or "warning" in r.stderr:
+        raise RuntimeError(f"g++ failed on {STRATEGY_SRC}:\n{r.stderr}")
+    os.replace(exe + ".tmp", exe)
+    return exe
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--force", action="store_true")

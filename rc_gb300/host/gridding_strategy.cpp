@@ -1,5 +1,6 @@
 // The gridding strategy of MS6/programs/gridding.hs:40-103, restated on the
-// C++ host layer (include/rc_kernels.hpp) for the parity tests: for every
+// C++ host layer (include/rc_kernels.hpp) for the parity tests and the
+// drop-in timing of the benchmark: for every
 // (u, v) tile, binSizer + binner, gridInit, one gridKernel per w-bin with
 // the bin's GCF (gcfKernel), gridDetiling into the full grid; then ifftKern.
 // With a model grid it also degrids every binned visibility (degridKernel),
@@ -8,7 +9,13 @@
 // cleanResidual); `rotate` phase-rotates them to a facet (rotateKernel);
 // `oskar` reads an OSKAR file's records (readOskarData, oskarReader).
 //
-// usage: gridding_strategy DIR MODE     MODE = bins | grid | degrid | clean | rotate | oskar
+// `time` runs gridding (every tile's w-bins, detiled into the full grid) and
+// degridding (every binned visibility against the model grid) K times after W
+// warm-up passes, the binning and the GCF reads done once beforehand (they
+// belong to the observation, not to a pass), and prints one JSON line of
+// per-pass wall times.
+//
+// usage: gridding_strategy DIR MODE     MODE = bins | grid | degrid | clean | rotate | oskar | time
 //   DIR/params.txt   width height theta tiles bins n_gcf grid_kernel degrid_kernel
 //                    then n_gcf lines "file size w"
 //   DIR/vis.bin      N x 5 doubles (u v w re im)
@@ -16,10 +23,12 @@
 //   DIR/clean.txt    gain threshold (clean)
 //   DIR/rotate.txt   facets lon lat l_low m_low (rotate)
 //   DIR/oskar.txt    file freq pol low high (oskar)
+//   DIR/time.txt     warmup steps (time; needs DIR/model.bin)
 // writes DIR/bins.bin (per tile, per bin: low high count, then the binned
 // records), DIR/grid.bin, DIR/image.bin, DIR/pred.bin (the degridded records
 // in tile, bin order), DIR/clean_model.bin + DIR/clean_residual.bin,
 // DIR/rot.bin, DIR/oskar.bin.
+#include <chrono>
 #include <cstdio>
 #include <string>
 #include <vector>
@@ -37,7 +46,8 @@ static std::vector<double> read_doubles(const std::string& path) {
   return v;
 }
 
-static void write_doubles(const std::string& path, const std::vector<double>& v) {
+template <class V>
+static void write_doubles(const std::string& path, const V& v) {
   FILE* f = std::fopen(path.c_str(), "wb");
   if (!f) throw rc::KernelError("cannot write " + path, -1);
   std::fwrite(v.data(), sizeof(double), v.size(), f);
@@ -63,6 +73,86 @@ static rc::UVGrid grid_tiles(rc::GridKernelType kt, const rc::GridPar& gp, const
       rc::gridDetiling(tile, full);
     }
   return full;
+}
+
+static double now_ms() {
+  using namespace std::chrono;
+  return duration<double, std::milli>(steady_clock::now().time_since_epoch()).count();
+}
+
+// `time` mode: the gridding and degridding passes of the strategy, timed.
+static void time_passes(const std::string& dir, rc::GridKernelType gkt, rc::DegridKernelType dkt,
+                        const rc::GridPar& gp, const rc::GCFPar& gcfp, const rc::Vis& vis,
+                        rc::UVGrid& model) {
+  int warmup = 1, steps = 3;
+  FILE* tf = std::fopen((dir + "/time.txt").c_str(), "r");
+  if (!tf || std::fscanf(tf, "%d %d", &warmup, &steps) != 2)
+    throw rc::KernelError("bad time.txt", -1);
+  std::fclose(tf);
+  struct Region {
+    rc::Range u, v;
+    std::vector<rc::VisBin> vb;
+    std::vector<rc::GCFs> g;
+  };
+  // the observation's regions: binSizer + binner per tile, then the GCF reads
+  const double tb0 = now_ms();
+  std::vector<Region> regions;
+  for (int tv = 0; tv < gp.tiles; tv++)
+    for (int tu = 0; tu < gp.tiles; tu++) {
+      Region r;
+      r.u = {tu * gp.width / gp.tiles, (tu + 1) * gp.width / gp.tiles};
+      r.v = {tv * gp.height / gp.tiles, (tv + 1) * gp.height / gp.tiles};
+      r.vb = rc::binner(gp, vis, r.u, r.v, rc::binSizer(gp, vis, r.u, r.v));
+      regions.push_back(std::move(r));
+    }
+  const double tb1 = now_ms();
+  long long calls = 0, records = 0;
+  for (Region& r : regions)
+    for (rc::VisBin& b : r.vb) {
+      r.g.push_back(b.vis.size() ? rc::gcfKernel(gcfp, b.bin) : rc::GCFs{});
+      if (b.vis.size()) {
+        calls++;
+        records += b.vis.size();
+      }
+    }
+  const double tb2 = now_ms();
+  std::vector<double> t_grid, t_degrid;
+  rc::UVGrid full;
+  std::vector<double> pred_out;
+  for (int it = 0; it < warmup + steps; it++) {
+    const double t0 = now_ms();
+    full = rc::gridInitDetile({0, gp.width}, {0, gp.height});
+    for (Region& r : regions) {
+      rc::UVGrid tile = rc::gridInit(gcfp, r.u, r.v);
+      for (size_t k = 0; k < r.vb.size(); k++)
+        if (r.vb[k].vis.size()) rc::gridKernel(gkt, gp, gcfp, r.vb[k], r.g[k], tile);
+      rc::gridDetiling(tile, full);
+    }
+    const double t1 = now_ms();
+    pred_out.clear();
+    for (Region& r : regions)
+      for (size_t k = 0; k < r.vb.size(); k++)
+        if (r.vb[k].vis.size()) {
+          const rc::Vis out = rc::degridKernel(dkt, gp, gcfp, r.g[k], model, r.vb[k].vis);
+          pred_out.insert(pred_out.end(), out.rec.begin(), out.rec.end());
+        }
+    const double t2 = now_ms();
+    if (it >= warmup) {
+      t_grid.push_back(t1 - t0);
+      t_degrid.push_back(t2 - t1);
+    }
+  }
+  write_doubles(dir + "/grid.bin", full.data);
+  write_doubles(dir + "/pred.bin", pred_out);
+  auto list = [](const std::vector<double>& v) {
+    std::string s = "[";
+    for (size_t i = 0; i < v.size(); i++) s += (i ? ", " : "") + std::to_string(v[i]);
+    return s + "]";
+  };
+  std::printf(
+      "{\"bin_ms\": %.3f, \"gcf_read_ms\": %.3f, \"calls_per_direction\": %lld, "
+      "\"records\": %lld, \"grid_ms\": %s, \"degrid_ms\": %s}\n",
+      tb1 - tb0, tb2 - tb1, calls, records, list(t_grid).c_str(), list(t_degrid).c_str());
 }
 
 int main(int argc, char** argv) {
@@ -109,14 +199,19 @@ int main(int argc, char** argv) {
     rc::Vis vis;
     vis.rec = read_doubles(dir + "/vis.bin");
     rc::UVGrid model;
-    if (mode == "degrid") {
+    if (mode == "degrid" || mode == "time") {
       model.width = gp.width;
       model.height = gp.height;
-      model.data = read_doubles(dir + "/model.bin");
+      const std::vector<double> m = read_doubles(dir + "/model.bin");
+      model.data.assign(m.begin(), m.end());
       if (model.data.size() != (size_t)2 * gp.width * gp.height)
         throw rc::KernelError("bad model.bin", -1);
     }
 
+    if (mode == "time") {
+      time_passes(dir, gkt, dkt, gp, gcfp, vis, model);
+      return 0;
+    }
     if (mode == "grid") {
       rc::UVGrid full = grid_tiles(gkt, gp, gcfp, vis);
       write_doubles(dir + "/grid.bin", full.data);

@@ -227,6 +227,17 @@ def config(name: str, seed: int | None = None, n_t: int | None = None) -> Observ
     return _finish(name, rng, uvw_m, [150e6], 512, 8, 8, 32)
 
 
+def abi_gcf_files(ob: Observation):
+    """GCF files for driving the reference-ABI strategy on a workload whose
+    plane supports follow S = 8 + 56 sqrt(|w| / w_max): the reference's own
+    support set 16 / 32 / 64 (MS6/cfg/continuum.yaml) with each file's w at
+    the point where the rule passes the previous size, so that gcfGet's choice
+    (the largest file w <= the bin's largest |w|) never has a smaller support
+    than the rule asks for below the next file.  [(w, support)]."""
+    wmax = max(abs(ob.w_low), abs(ob.w_high))
+    return [(0.0, 16), (wmax * (8.0 / 56.0) ** 2, 32), (wmax * (24.0 / 56.0) ** 2, 64)]
+
+
 def write_oskar_vis(path, ob: Observation, max_times_per_block: int = 8,
                     freq_hz: float = 150e6) -> int:
     """Store a single-channel observation as an OSKAR 2.6 visibility file, the

@@ -1,4 +1,4 @@
-"""Helpers of the C++ host-layer tests: build tests/cpp/gridding_strategy.cpp
+"""Helpers of the C++ host-layer tests: build rc_gb300/host/gridding_strategy.cpp
 against include/rc_kernels.hpp and librc_gb300.so, and lay out its inputs."""
 import os
 import subprocess
@@ -13,21 +13,13 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 def build_program(out_dir, ms5=False):
     """ms5: against librc_gb300_ms5.so with -DGB_MS5_ABI (MS5's bindings)."""
+    from rc_gb300 import build as B
+
     if ms5:
         lib.load_ms5()  # builds librc_gb300_ms5.so if needed
     else:
         lib.load()  # builds librc_gb300.so if needed
-    libdir = os.path.join(ROOT, "rc_gb300")
-    exe = os.path.join(str(out_dir), "gridding_strategy_ms5" if ms5 else "gridding_strategy")
-    cmd = ["g++", "-std=c++17", "-O2", "-Wall", "-Wextra", "-I", os.path.join(ROOT, "include"),
-           os.path.join(ROOT, "tests", "cpp", "gridding_strategy.cpp"), "-L", libdir,
-           "-lrc_gb300_ms5" if ms5 else "-lrc_gb300", "-Wl,-rpath," + libdir, "-o", exe]
-    if ms5:
-        cmd.insert(1, "-DGB_MS5_ABI")
-    r = subprocess.run(cmd, capture_output=True, text=True)
-    assert r.returncode == 0, r.stderr
-    assert "warning" not in r.stderr, r.stderr
-    return exe
+    return B.strategy_program(str(out_dir), ms5=ms5)
 
 
 def write_case(d, G, theta, tiles, bins, vis5, gcf_files, gk=1, dk=1, model=None):

@@ -1,5 +1,5 @@
 """The gridding strategy of MS6/programs/gridding.hs run through the C++ host
-layer (include/rc_kernels.hpp, tests/cpp/gridding_strategy.cpp) on the GPU,
+layer (include/rc_kernels.hpp, rc_gb300/host/gridding_strategy.cpp) on the GPU,
 against the same strategy composed from the oracle: per (u, v) tile, the
 oracle's binSizer + binner, kern_scatter semantics per w-bin with the GCF
 that gcfGet picks (conjugated for negative w) into the tile with its margin,

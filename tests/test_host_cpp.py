@@ -107,3 +107,24 @@ def test_binning_of_empty_tiles(exe, tmp_path):
             empty += low == 0.0 and high == 0.0 and count == 0 and n == 0
             k += 4 + 5 * n
     assert k == len(got) and empty == 9  # three empty tiles x three bins
+
+
+def test_vectorised_binning_equals_the_loop_restatement():
+    """oracle.tile_bins_vec (used by the full-size strategy test) gives the same
+    bins, counts and records, bit for bit, as the loop restatement tile_bins,
+    on tiles with edge visibilities, duplicate w values and a zero-width w range."""
+    vis5 = H.synthetic(11, 4000, G, THETA, 60.0)
+    edges = [H.O.xy2uv(G, THETA, z) for z in (0, 128, 256)]
+    vis5[:30, 0] = np.repeat(edges, 10)
+    vis5[40:400, 2] = np.round(vis5[40:400, 2])  # many equal w values
+    first = (vis5[:, 0] < edges[1]) & (vis5[:, 1] < edges[1])
+    vis5[first, 2] = 0.0
+    for bins in (1, 3, 7):
+        for v in H.tiles_of(G, 2):
+            for u in H.tiles_of(G, 2):
+                a = H.O.tile_bins(vis5, G, THETA, u, v, bins)
+                b = H.O.tile_bins_vec(vis5, G, THETA, u, v, bins)
+                assert len(a) == len(b)
+                for (l1, h1, c1, r1), (l2, h2, c2, r2) in zip(a, b):
+                    assert l1 == l2 and h1 == h2 and c1 == c2
+                    assert np.array_equal(r1, r2)
