@@ -167,9 +167,10 @@ static int batch_build(gb_batch* B, int32_t n, const gb_batch_member* m, cudaStr
   for (int i = 0; i < n; i++) {
     gb_plan* p = B->members[i];
     for (HostItem h : p->host_items) {
-      const int u = (int)(std::lower_bound(widths.begin(), widths.end(), p->cls[h.it.cls].L) -
+      const int u = (int)(std::lower_bound(widths.begin(), widths.end(),
+                                           p->cls[item_class(h.it.cls)].L) -
                           widths.begin());
-      h.it.cls = (int16_t)u;
+      h.it.cls = (int16_t)((h.it.cls & ~kItemClassMask) | u);
       h.it.start += (int32_t)off;
       h.grid = i;
       items.push_back(h);

@@ -391,6 +391,7 @@ extern "C" int gb_grid_f32_noalloc(const gb_geometry* geo, int64_t n_vis, const 
   D.uvw = d_uvw;
   D.uvw_stride = uvw_stride;
   D.plane = plane_of;
+  D.order = nullptr;
   D.supports = nullptr;
   D.gcf_offsets = nullptr;
   D.scale = geo->scale;

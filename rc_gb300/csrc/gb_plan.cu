@@ -28,6 +28,7 @@ __global__ void k_plan_count(PlanDev P, const PlaneInfo* __restrict__ pl,
                              const int32_t* __restrict__ plane_in, int32_t* __restrict__ plane_out,
                              int32_t n_planes, double w_lo, double w_hi, int32_t T, int32_t ntx,
                              int32_t nper, int32_t* __restrict__ hist,
+                             int32_t* __restrict__ vis_hist,
                              unsigned long long* __restrict__ counters) {
   __shared__ unsigned long long s_kept, s_taps, s_recs, s_paired;
   if (threadIdx.x == 0) s_kept = s_taps = s_recs = s_paired = 0ull;
@@ -39,11 +40,19 @@ __global__ void k_plan_count(PlanDev P, const PlaneInfo* __restrict__ pl,
     int32_t p = plane_in ? plane_in[t] : w_plane(r[2], w_lo, w_hi, n_planes);
     if (p >= n_planes) p = -1;
     plane_out[t] = p;
-    if (p < 0) continue;
+    const int64_t ntiles = (int64_t)ntx * ((P.ext_y + T - 1) / T);
+    if (p < 0) {
+      atomicAdd(&vis_hist[ntiles], 1);  // skipped visibilities go last
+      continue;
+    }
     const PlaneInfo q = pl[p];
     const VisIndex ix =
         vis_index(r[0], r[1], P.scale, P.grid_size, q.S, P.margin, 0, 0, P.ext_x, P.ext_y);
-    if (!ix.keep) continue;
+    if (!ix.keep) {
+      atomicAdd(&vis_hist[ntiles], 1);
+      continue;
+    }
+    atomicAdd(&vis_hist[(int64_t)(ix.y0 / T) * ntx + ix.x0 / T], 1);
     kept++;
     taps += (unsigned long long)q.S * q.S;
     for (int ky = 0; ky < q.k; ky++) {
@@ -78,15 +87,23 @@ __global__ void k_plan_count(PlanDev P, const PlaneInfo* __restrict__ pl,
 
 __global__ void k_plan_fill(PlanDev P, const PlaneInfo* __restrict__ pl, int32_t T, int32_t ntx,
                             int32_t nper, const int32_t* __restrict__ offs,
-                            int32_t* __restrict__ cursor, Rec* __restrict__ recs) {
+                            int32_t* __restrict__ cursor, Rec* __restrict__ recs,
+                            const int32_t* __restrict__ vis_offs,
+                            int32_t* __restrict__ vis_cursor, int32_t* __restrict__ order) {
+  const int64_t ntiles = (int64_t)ntx * ((P.ext_y + T - 1) / T);
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < P.n_vis;
        t += (int64_t)gridDim.x * blockDim.x) {
     const int32_t p = P.plane[t];
-    if (p < 0) continue;
+    if (p < 0) {
+      order[vis_offs[ntiles] + atomicAdd(&vis_cursor[ntiles], 1)] = (int32_t)t;
+      continue;
+    }
     const PlaneInfo q = pl[p];
     const double* r = P.uvw + t * P.uvw_stride;
     const VisIndex ix =
         vis_index(r[0], r[1], P.scale, P.grid_size, q.S, P.margin, 0, 0, P.ext_x, P.ext_y);
+    const int64_t vt = ix.keep ? (int64_t)(ix.y0 / T) * ntx + ix.x0 / T : ntiles;
+    order[vis_offs[vt] + atomicAdd(&vis_cursor[vt], 1)] = (int32_t)t;
     if (!ix.keep) continue;
     const int64_t gbase = q.gcf_off + (int64_t)ix.phase * q.S * q.S;
     for (int ky = 0; ky < q.k; ky++) {
@@ -160,6 +177,7 @@ static int blocks_for(int64_t n, int threads) {
 static void free_plan(gb_plan* p) {
   if (!p) return;
   cudaFree(p->d_plane);
+  cudaFree(p->d_order);
   cudaFree(p->d_supports);
   cudaFree(p->d_offsets);
   cudaFree(p->d_planes);
@@ -187,13 +205,13 @@ void make_bundles(const std::vector<HostItem>& items, const ClassInfo* cls, int 
   for (const auto& h : items) max_grid = std::max(max_grid, h.grid);
   const size_t ng = (size_t)max_grid + 1, nb = (size_t)n_classes * ng;
   std::vector<size_t> first(nb + 1, 0);
-  for (const auto& h : items) first[(size_t)h.it.cls * ng + h.grid + 1]++;
+  for (const auto& h : items) first[(size_t)item_class(h.it.cls) * ng + h.grid + 1]++;
   for (size_t k = 1; k <= nb; k++) first[k] += first[k - 1];
   std::vector<int32_t> order(items.size());
   {
     std::vector<size_t> next(first.begin(), first.end() - 1);
     for (size_t i = 0; i < items.size(); i++)
-      order[next[(size_t)items[i].it.cls * ng + items[i].grid]++] = (int32_t)i;
+      order[next[(size_t)item_class(items[i].it.cls) * ng + items[i].grid]++] = (int32_t)i;
   }
   // within a bucket, longest first; groups of G items form a bundle
   struct HB {
@@ -230,6 +248,27 @@ void make_bundles(const std::vector<HostItem>& items, const ClassInfo* cls, int 
   b_out.reserve(bundles.size());
   for (auto& hb : bundles) b_out.push_back(hb.b);
 }
+
+// Modelled shared-memory wavefronts per pair that degridding's split-row stage
+// costs a sub-warp of SW lanes reading SW consecutive pairs (row-major, rows
+// of w2 pairs) with rows r (mod 16) float2 apart: the largest number of
+// addresses on one 8-byte bank pair (of 16), averaged over where the run
+// starts in its row, per pair of the run.
+static double split_stage_cost(int w2, int r, int SW) {
+  double sum = 0;
+  for (int t0 = 0; t0 < w2; t0++) {
+    int cnt[16] = {0};
+    for (int l = 0; l < SW; l++) {
+      const int t = t0 + l, j = t / w2, i = t - j * w2;
+      cnt[(j * r + i) & 15]++;
+    }
+    sum += *std::max_element(cnt, cnt + 16);
+  }
+  return sum / w2 / SW;
+}
+
+// Sub-warp width of degridding for a class's largest period (the kernel's rule).
+static int degrid_subwarp(int pmax) { return pmax <= 8 ? 8 : pmax <= 16 ? 16 : 32; }
 
 static int build_plan(gb_plan* P, const gb_geometry* geo, int64_t n_vis, const double* d_uvw,
                       int64_t uvw_stride, const int32_t* d_plane_in, cudaStream_t s) {
@@ -298,7 +337,8 @@ static int build_plan(gb_plan* P, const gb_geometry* geo, int64_t n_vis, const d
   for (int st = 0; st < 3; st++) P->ctas_per_sm_degrid[st] = tiled_ctas_per_sm(P, false, st);
 
   // ---- device tables
-  if ((rc = dalloc(&P->d_plane, n_vis)) || (rc = dalloc(&P->d_supports, np)) ||
+  if ((rc = dalloc(&P->d_plane, n_vis)) || (rc = dalloc(&P->d_order, n_vis)) ||
+      (rc = dalloc(&P->d_supports, np)) ||
       (rc = dalloc(&P->d_offsets, np)) || (rc = dalloc(&P->d_planes, np)) ||
       (rc = dalloc(&P->d_queue, 3)))
     return rc;
@@ -316,6 +356,7 @@ static int build_plan(gb_plan* P, const gb_geometry* geo, int64_t n_vis, const d
   D.uvw = d_uvw;
   D.uvw_stride = uvw_stride;
   D.plane = P->d_plane;
+  D.order = P->d_order;
   D.supports = P->d_supports;
   D.gcf_offsets = P->d_offsets;
   D.scale = geo->scale;
@@ -333,33 +374,42 @@ static int build_plan(gb_plan* P, const gb_geometry* geo, int64_t n_vis, const d
     gb_set_error(GB_ERR_CAPACITY, "too many (tile, period) bins");
     return GB_ERR_CAPACITY;
   }
-  int32_t *d_hist = nullptr, *d_offs = nullptr;
+  // per-visibility order: one bucket per tile (the footprint corner's) and a
+  // last one for the visibilities no kernel grids
+  const int64_t nvkeys = (int64_t)P->ntx * P->nty + 1;
+  int32_t *d_hist = nullptr, *d_offs = nullptr, *d_vhist = nullptr, *d_voffs = nullptr;
   unsigned long long* d_cnt = nullptr;
   if ((rc = dalloc(&d_hist, nkeys)) || (rc = dalloc(&d_offs, nkeys + 1)) ||
+      (rc = dalloc(&d_vhist, nvkeys)) || (rc = dalloc(&d_voffs, nvkeys)) ||
       (rc = dalloc(&d_cnt, 4))) {
     cudaFree(d_hist);
     cudaFree(d_offs);
+    cudaFree(d_vhist);
+    cudaFree(d_voffs);
     cudaFree(d_cnt);
     return rc;
   }
   struct Tmp {
-    void* p[3];
+    void* p[5];
     ~Tmp() {
       for (void* q : p) cudaFree(q);
     }
-  } tmp{{d_hist, d_offs, d_cnt}};
+  } tmp{{d_hist, d_offs, d_vhist, d_voffs, d_cnt}};
   GB_CUDA_TRY(cudaMemsetAsync(d_hist, 0, sizeof(int32_t) * nkeys, s));
+  GB_CUDA_TRY(cudaMemsetAsync(d_vhist, 0, sizeof(int32_t) * nvkeys, s));
   GB_CUDA_TRY(cudaMemsetAsync(d_cnt, 0, sizeof(unsigned long long) * 4, s));
   if (n_vis > 0) {
     k_plan_count<<<blocks_for(n_vis, 256), 256, 0, s>>>(
         D, P->d_planes, d_plane_in, P->d_plane, np, geo->w_low, geo->w_high, P->T, P->ntx, nper,
-        d_hist, d_cnt);
+        d_hist, d_vhist, d_cnt);
     GB_CUDA_TRY(cudaGetLastError());
   }
-  std::vector<int32_t> hist(nkeys);
+  std::vector<int32_t> hist(nkeys), vhist(nvkeys);
   unsigned long long cnt[4];
   GB_CUDA_TRY(cudaMemcpyAsync(hist.data(), d_hist, sizeof(int32_t) * nkeys, cudaMemcpyDeviceToHost,
                               s));
+  GB_CUDA_TRY(cudaMemcpyAsync(vhist.data(), d_vhist, sizeof(int32_t) * nvkeys,
+                              cudaMemcpyDeviceToHost, s));
   GB_CUDA_TRY(cudaMemcpyAsync(cnt, d_cnt, sizeof(cnt), cudaMemcpyDeviceToHost, s));
   GB_CUDA_TRY(cudaStreamSynchronize(s));
   P->kept = (int64_t)cnt[0];
@@ -406,7 +456,32 @@ static int build_plan(gb_plan* P, const gb_geometry* geo, int64_t n_vis, const d
     r_lo[rank_cls[r]] = std::min(r_lo[rank_cls[r]], r);
     r_hi[rank_cls[r]] = std::max(r_hi[rank_cls[r]], r + 1);
   }
+  // split-row stride residue per item: the residue that minimises the
+  // modelled stage cost of its largest run (pieces of period P pair P / 2 taps
+  // per row when P is even; choosing for the largest run alone comes within
+  // 1 % of minimising over all of an item's runs on the benchmark workloads)
+  std::vector<int> rank_residue(nper, -1);
+  for (int r = 0; r < nper; r++) {
+    const int Pr = periods[r], SW = degrid_subwarp(P->cls[rank_cls[r]].pmax);
+    if (Pr & 1) continue;
+    double bc = 0;
+    for (int m = 0; m < 16; m++) {
+      const double c = split_stage_cost(Pr / 2, m, SW);
+      if (rank_residue[r] < 0 || c < bc) {
+        rank_residue[r] = m;
+        bc = c;
+      }
+    }
+  }
   std::vector<HostItem> items;
+  int64_t top_taps = 0;
+  int top_rank = -1;
+  auto close_item = [&](HostItem& h) {
+    h.it.cls = item_cls_with_residue(h.it.cls, top_rank < 0 ? -1 : rank_residue[top_rank]);
+    top_taps = 0;
+    top_rank = -1;
+    items.push_back(h);
+  };
   int64_t tiles_used = 0;
   for (int64_t tile = 0; tile < (int64_t)P->ntx * P->nty; tile++) {
     const int64_t k0 = tile * nper;
@@ -439,14 +514,18 @@ static int build_plan(gb_plan* P, const gb_geometry* geo, int64_t n_vis, const d
           cur.it.count += take;
           cur.it.pmax = (int16_t)std::max<int>(cur.it.pmax, periods[r]);
           cur.cost += take * rcst;
+          if ((int64_t)take * periods[r] * periods[r] > top_taps) {
+            top_taps = (int64_t)take * periods[r] * periods[r];
+            top_rank = r;
+          }
           pos += take;
           if (cur.cost >= cmax) {
-            items.push_back(cur);
+            close_item(cur);
             open = false;
           }
         }
       }
-      if (open) items.push_back(cur);
+      if (open) close_item(cur);
     }
   }
   P->tiles_used = tiles_used;
@@ -467,15 +546,27 @@ static int build_plan(gb_plan* P, const gb_geometry* geo, int64_t n_vis, const d
   GB_CUDA_TRY(cudaMemcpyAsync(d_offs, offs.data(), sizeof(int32_t) * (nkeys + 1),
                               cudaMemcpyHostToDevice, s));
   GB_CUDA_TRY(cudaMemsetAsync(d_hist, 0, sizeof(int32_t) * nkeys, s));  // reused as cursor
+  std::vector<int32_t> voffs(nvkeys);
+  {
+    int64_t a = 0;
+    for (int64_t k = 0; k < nvkeys; k++) {
+      voffs[k] = (int32_t)a;
+      a += vhist[k];
+    }
+  }
+  GB_CUDA_TRY(cudaMemcpyAsync(d_voffs, voffs.data(), sizeof(int32_t) * nvkeys,
+                              cudaMemcpyHostToDevice, s));
+  GB_CUDA_TRY(cudaMemsetAsync(d_vhist, 0, sizeof(int32_t) * nvkeys, s));  // reused as cursor
   if (P->n_items)
     GB_CUDA_TRY(cudaMemcpyAsync(P->d_items, it_sorted.data(), sizeof(Item) * P->n_items,
                                 cudaMemcpyHostToDevice, s));
   if (P->n_bundles)
     GB_CUDA_TRY(cudaMemcpyAsync(P->d_bundles, bvec.data(), sizeof(Bundle) * P->n_bundles,
                                 cudaMemcpyHostToDevice, s));
-  if (n_vis > 0 && P->n_recs > 0) {
+  if (n_vis > 0) {
     k_plan_fill<<<blocks_for(n_vis, 256), 256, 0, s>>>(D, P->d_planes, P->T, P->ntx, nper, d_offs,
-                                                       d_hist, P->d_recs);
+                                                       d_hist, P->d_recs, d_voffs, d_vhist,
+                                                       P->d_order);
     GB_CUDA_TRY(cudaGetLastError());
   }
   GB_CUDA_TRY(cudaStreamSynchronize(s));

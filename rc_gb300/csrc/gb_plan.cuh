@@ -3,6 +3,8 @@
 //
 // Layout in HBM (per plan):
 //   plane[n_vis]        int32  w-plane of each visibility (or -1)
+//   order[n_vis]        int32  visibilities sorted by the tile of their corner
+//                              (the visit order of the plain FP64 kernels)
 //   recs[n_recs]        Rec    16-byte records sorted by (grid tile, period)
 //   items[n_items]      Item   a contiguous record range of one tile and one
 //                              thread-group class
@@ -29,6 +31,8 @@ struct PlanDev {
   const double* uvw;
   int64_t uvw_stride;
   const int32_t* plane;        // per visibility
+  const int32_t* order;        // the visibilities by the grid tile of their footprint
+                               // corner (kept ones first), or NULL: index order
   const int32_t* supports;     // per plane
   const int64_t* gcf_offsets;  // per plane
   double scale;
@@ -50,7 +54,8 @@ static_assert(sizeof(Rec) == 16, "Rec must be 16 bytes");
 struct __align__(16) Item {
   int32_t start, count;    // record range
   int16_t tile_x, tile_y;  // tile indices
-  int16_t pmax, cls;       // largest period in the item, thread-group class
+  int16_t pmax, cls;       // largest period in the item; thread-group class and
+                           // split-row stride residue (item_class, item_stride_residue)
 };
 static_assert(sizeof(Item) == 16, "Item must be 16 bytes");
 
@@ -90,8 +95,25 @@ __host__ __device__ inline size_t grid_group_bytes(int A, int L) {
 // (a TMA box row must be a multiple of 16 bytes) and starts each group's
 // region on a 128-byte boundary (TMA destination).
 __host__ __device__ inline int stage_stride(int A) { return (A + 1) & ~1; }
+// The split-row stage may lay its rows further apart than stage_stride: an
+// item's row stride is stage_stride + ((r - stage_stride) mod 16) float2 for
+// the residue r (0..15) its plan chose, so that a sub-warp reading pairs
+// row-major across row ends, rows of w2 pairs, hits the 16 eight-byte bank
+// pairs evenly when r = w2 mod 16 (up to 15 more pixels per row).
+__host__ __device__ inline int split_row_stride(int A, int r) {
+  const int Ae = stage_stride(A);
+  return r < 0 ? Ae : Ae + ((r - Ae) & 15);
+}
 __host__ __device__ inline size_t degrid_stage_bytes(int A) {
-  return (8 * (size_t)A * stage_stride(A) + 127) & ~(size_t)127;
+  return (8 * (size_t)A * (stage_stride(A) + 15) + 127) & ~(size_t)127;
+}
+// Item.cls packs the thread-group class (bits 0-3) and the split-row stride
+// residue of degridding plus one (bits 4-8; 0: the plain stage_stride).
+constexpr int kItemClassMask = 0xF;
+__host__ __device__ inline int item_class(int16_t cls) { return cls & kItemClassMask; }
+__host__ __device__ inline int item_stride_residue(int16_t cls) { return ((cls >> 4) & 31) - 1; }
+__host__ __device__ inline int16_t item_cls_with_residue(int16_t cls, int split_r) {
+  return (int16_t)((cls & kItemClassMask) | ((split_r + 1) << 4));
 }
 __host__ __device__ inline size_t degrid_group_bytes(int A, int L) {
   return degrid_stage_bytes(A) + 32 * (size_t)L;
@@ -156,6 +178,7 @@ struct gb_plan {
   int ctas_per_sm_degrid[3] = {1, 1, 1};  // per GB_STAGE_* form
   // device arrays owned by the plan
   int32_t* d_plane = nullptr;
+  int32_t* d_order = nullptr;
   int32_t* d_supports = nullptr;
   int64_t* d_offsets = nullptr;
   gb::PlaneInfo* d_planes = nullptr;

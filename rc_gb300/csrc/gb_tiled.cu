@@ -474,15 +474,18 @@ __device__ __forceinline__ void degrid_item(const TiledArgs& a, const Item& it, 
   const float2* __restrict__ grid = gs.grid;
   float2* __restrict__ pred = gs.vis;
   constexpr bool TMA = STAGE == kStageTma, SPLIT = STAGE == kStageSplit;
-  const int Ae = stage_stride(A);  // stage row stride (even)
-  // TMA and ROWS stage rows as they lie in the grid.  SPLIT stores each row
-  // as its even pixels, then its odd pixels (He = Ae / 2 each), so the two
-  // taps of a pair are read by two loads that are each contiguous across the
-  // lanes, whatever the parity of the piece's first column.
+  const int Ae = stage_stride(A);  // pixels staged per row (even)
+  // TMA and ROWS stage rows as they lie in the grid, Ae apart.  SPLIT stores
+  // each row as its even pixels, then its odd pixels (He = Ae / 2 each), so
+  // the two taps of a pair are read by two loads that are each contiguous
+  // across the lanes, whatever the parity of the piece's first column; its
+  // rows are Rs apart, Rs chosen by the plan for the item's piece widths
+  // (split_row_stride) so that row-major pair runs spread over the banks.
   const int He = Ae >> 1;
+  const int Rs = SPLIT ? split_row_stride(A, item_stride_residue(it.cls)) : Ae;
   const int x0 = it.tile_x * a.T, y0 = it.tile_y * a.T;
   // array sizes for the bounds-checked build (unused otherwise)
-  const int stage_len = A * Ae;
+  const int stage_len = A * Rs;
 #ifdef GB_CHECKED
   const int64_t gcf_len = a.gcf_len;
 #else
@@ -507,7 +510,7 @@ __device__ __forceinline__ void degrid_item(const TiledArgs& a, const Item& it, 
     for (int q = lt; q < AA; q += L) {
       const int gx = x0 + px, gy = y0 + py;
       const bool in = px < A && gx < gs.ext_x && gy < gs.ext_y;
-      const int sq = SPLIT ? py * Ae + (px & 1) * He + (px >> 1) : q;
+      const int sq = SPLIT ? py * Rs + (px & 1) * He + (px >> 1) : q;
       px += dx;
       py += dy;
       if (px >= Ae) {
@@ -515,7 +518,7 @@ __device__ __forceinline__ void degrid_item(const TiledArgs& a, const Item& it, 
         py++;
       }
       const float2* src = in ? grid + (int64_t)gy * gs.pitch + gx : grid;
-      const unsigned dst = (unsigned)__cvta_generic_to_shared(sg + GB_IDX(sq, AA));
+      const unsigned dst = (unsigned)__cvta_generic_to_shared(sg + GB_IDX(sq, stage_len));
       asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(dst), "l"(src),
                    "r"(in ? 8 : 0)
                    : "memory");
@@ -550,7 +553,7 @@ __device__ __forceinline__ void degrid_item(const TiledArgs& a, const Item& it, 
       // stage offset of the piece's first tap (row-major), or in the split
       // layout: of its first tap for pairs, of its first row for single taps
       if constexpr (SPLIT)
-        d.q0 = r.yl * Ae + (paired ? (r.xl & 1) * He + (r.xl >> 1) : 0);
+        d.q0 = r.yl * Rs + (paired ? (r.xl & 1) * He + (r.xl >> 1) : 0);
       else
         d.q0 = r.yl * Ae + r.xl;
       srec[lt] = d;
@@ -603,7 +606,7 @@ __device__ __forceinline__ void degrid_item(const TiledArgs& a, const Item& it, 
 #pragma unroll
             for (int u = 0; u < UN; u++) {
               off_g[u] = j * p2 + i;
-              off_s[u] = j * Ae + (SPLIT ? i : 2 * i);
+              off_s[u] = j * Rs + (SPLIT ? i : 2 * i);
               i += di;
               j += dj;
               if (i >= w2) {
@@ -651,7 +654,7 @@ __device__ __forceinline__ void degrid_item(const TiledArgs& a, const Item& it, 
               off_g[u] = j * pitch + i;
               if constexpr (SPLIT) {
                 const int c = xl + i;
-                off_s[u] = j * Ae + (c & 1) * He + (c >> 1);
+                off_s[u] = j * Rs + (c & 1) * He + (c >> 1);
               } else {
                 off_s[u] = j * Ae + i;
               }
