@@ -118,7 +118,17 @@ __global__ void k_plan_fill(PlanDev P, const PlaneInfo* __restrict__ pl, int32_t
         const int wx = min(q.P, q.S - ox);
         const int tx = X0 / T, ty = Y0 / T;
         const int64_t key = ((int64_t)ty * ntx + tx) * nper + q.rank;
-        const int32_t pos = offs[key] + atomicAdd(&cursor[key], 1);
+        // lanes with the same bin take consecutive places in lane order (one
+        // atomic per bin and warp): neighbouring samples of a baseline, which
+        // a warp holds side by side, stay neighbours in the bin, where the
+        // gridder sums the taps that consecutive pieces put on one pixel
+        const unsigned act = __activemask();
+        const unsigned peers = __match_any_sync(act, key);
+        const int lane = threadIdx.x & 31, leader = __ffs(peers) - 1;
+        int32_t first = 0;
+        if (lane == leader) first = atomicAdd(&cursor[key], __popc(peers));
+        first = __shfl_sync(act, first, leader);
+        const int32_t pos = offs[key] + first + __popc(peers & ((1u << lane) - 1u));
         Rec rc;
         rc.vis = (int32_t)t;
         rc.gcf = (uint32_t)(gbase + (int64_t)oy * q.S + ox);

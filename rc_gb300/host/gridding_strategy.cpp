@@ -15,7 +15,12 @@
 // belong to the observation, not to a pass), and prints one JSON line of
 // per-pass wall times.
 //
-// usage: gridding_strategy DIR MODE     MODE = bins | grid | degrid | clean | rotate | oskar | time
+// `continuum` runs the major loop of MS6/programs/continuum.hs over these
+// kernels (fftKern, degridKernel, gridKernel, ifftKern, cleanModel,
+// cleanResidual) and writes the model and the final residual.
+//
+// usage: gridding_strategy DIR MODE
+//        MODE = bins | grid | degrid | clean | continuum | rotate | oskar | time
 //   DIR/params.txt   width height theta tiles bins n_gcf grid_kernel degrid_kernel
 //                    then n_gcf lines "file size w"
 //   DIR/vis.bin      N x 5 doubles (u v w re im)
@@ -24,10 +29,11 @@
 //   DIR/rotate.txt   facets lon lat l_low m_low (rotate)
 //   DIR/oskar.txt    file freq pol low high (oskar)
 //   DIR/time.txt     warmup steps (time; needs DIR/model.bin)
+//   DIR/continuum.txt  loops (continuum; with DIR/clean.txt)
 // writes DIR/bins.bin (per tile, per bin: low high count, then the binned
 // records), DIR/grid.bin, DIR/image.bin, DIR/pred.bin (the degridded records
 // in tile, bin order), DIR/clean_model.bin + DIR/clean_residual.bin,
-// DIR/rot.bin, DIR/oskar.bin.
+// DIR/rot.bin, DIR/oskar.bin, DIR/cont_model.bin + DIR/cont_residual.bin.
 #include <chrono>
 #include <cstdio>
 #include <string>
@@ -236,6 +242,59 @@ int main(int argc, char** argv) {
       write_doubles(dir + "/clean_residual.bin", rc::cleanResidual(cp, psf, dirty).data);
       return 0;
     }
+#ifndef GB_MS5_ABI  // MS5 binds no image -> grid transform (fftKern)
+    if (mode == "continuum") {
+      // the major loop of MS6/programs/continuum.hs:80-98: each iteration
+      // degrids the model's grid (fftKern) from the visibilities
+      // (degridModel: vis - D fft(model)), grids and images the result
+      // (idft of grid), and CLEANs it against the PSF of the visibilities:
+      // the model grows (cleanModel) until the last iteration, which returns
+      // the residual (cleanResidual against an empty model)
+      rc::CleanPar cp;
+      int loops = 0;
+      FILE* cf = std::fopen((dir + "/clean.txt").c_str(), "r");
+      if (!cf || std::fscanf(cf, "%lf %lf", &cp.gain, &cp.threshold) != 2)
+        throw rc::KernelError("bad clean.txt", -1);
+      std::fclose(cf);
+      FILE* lf = std::fopen((dir + "/continuum.txt").c_str(), "r");
+      if (!lf || std::fscanf(lf, "%d", &loops) != 1 || loops < 1)
+        throw rc::KernelError("bad continuum.txt", -1);
+      std::fclose(lf);
+      rc::Vis psf_vis = rc::psfVisKernel(vis);
+      rc::UVGrid g_psf = grid_tiles(gkt, gp, gcfp, psf_vis);
+      rc::Image psf = rc::ifftKern(gp, g_psf);
+      rc::Image mdl;
+      mdl.width = gp.width;
+      mdl.height = gp.height;
+      mdl.data.assign((size_t)gp.width * gp.height, 0.0);
+      rc::Image res;
+      for (int it = 0; it < loops; it++) {
+        rc::UVGrid mgrid = rc::fftKern(gp, mdl);
+        rc::Vis corrected;  // degridModel over every (u, v) tile and w-bin region
+        for (int tv = 0; tv < gp.tiles; tv++)
+          for (int tu = 0; tu < gp.tiles; tu++) {
+            const rc::Range u{tu * gp.width / gp.tiles, (tu + 1) * gp.width / gp.tiles};
+            const rc::Range v{tv * gp.height / gp.tiles, (tv + 1) * gp.height / gp.tiles};
+            std::vector<rc::VisBin> vb = rc::binner(gp, vis, u, v, rc::binSizer(gp, vis, u, v));
+            for (rc::VisBin& b : vb) {
+              if (b.vis.size() == 0) continue;
+              rc::GCFs g = rc::gcfKernel(gcfp, b.bin);
+              const rc::Vis o = rc::degridKernel(dkt, gp, gcfp, g, mgrid, b.vis);
+              corrected.rec.insert(corrected.rec.end(), o.rec.begin(), o.rec.end());
+            }
+          }
+        rc::UVGrid g_dirty = grid_tiles(gkt, gp, gcfp, corrected);
+        rc::Image dirty = rc::ifftKern(gp, g_dirty);
+        if (it + 1 < loops)
+          rc::cleanModel(cp, psf, dirty, mdl);
+        else
+          res = rc::cleanResidual(cp, psf, dirty);
+      }
+      write_doubles(dir + "/cont_model.bin", mdl.data);
+      write_doubles(dir + "/cont_residual.bin", res.data);
+      return 0;
+    }
+#endif
     if (mode == "rotate") {
       double lon = 0, lat = 0;
       int l_low = 0, m_low = 0;
