@@ -16,6 +16,7 @@
 
 #include <algorithm>
 #include <mutex>
+#include <type_traits>
 #include <thread>
 #include <vector>
 
@@ -647,6 +648,205 @@ static int df_prepare(const double* grid, int32_t ext_x, int32_t ext_y, int64_t 
   return GB_OK;
 }
 
+// ---------------------------------------------------------------- ABI gridding in shared memory
+// kern_scatter_gpu1 and its siblings for GCF sizes 16, 32 and 64.  A call's
+// kept records, counting-sorted by the kBlk x kBlk block of their footprint
+// corner (order_by_block), are cut into chunks of ScatShape<S>::CH
+// consecutive records, one CTA per chunk.  A CTA accumulates the records of
+// one block at a time in shared memory, over the block's footprint region
+// ((kBlk + S - 1)^2 pixels), in the degridders' double-float arithmetic
+// (products and sums err by about 2^-48 of their size); each thread owns the
+// region's pixels of its residues (x mod S, y mod S), so that every tap is an
+// exclusive read-modify-write, with no atomics.  When the block changes, the
+// non-zero pixels of the segment's footprints are added into the device grid
+// by FP64 atomics (regions of neighbouring blocks overlap, and a block's
+// records may span two chunks) and cleared.  With an Inf, a NaN or a
+// subnormal in the visibilities or the GCF, the chunk is gridded by the FP64
+// atomics of warp_scatter64 instead, so that those propagate as FP64 would.
+template <int S>
+struct ScatShape {
+  static constexpr int NT = S == 64 ? 512 : 256;  // threads per CTA
+  static constexpr int R = S * S / NT;            // residue slots per thread
+  static constexpr int DR = NT / S;               // residue rows between a thread's slots
+  static constexpr int CH = S == 16 ? 512 : S == 32 ? 256 : 128;  // records per CTA
+  static constexpr int RA = kBlk + S - 1;         // region edge (pixels)
+  static constexpr int As = (RA + 7) & ~7;        // region row stride (float4)
+};
+
+struct ScatRec {
+  float4 vis;      // (re hi, re lo, im hi, im lo) under the visibilities' scale
+  int32_t x0, y0;  // footprint corner relative to its block's origin (0 .. kBlk-1)
+  int32_t phase;   // GCF oversampling phase
+  int32_t key;     // block
+};
+
+template <int S>
+constexpr size_t scatter_blocks_smem() {
+  using Z = ScatShape<S>;
+  return sizeof(float4) * Z::RA * Z::As + sizeof(ScatRec) * Z::NT;
+}
+
+template <int S>
+__global__ void __launch_bounds__(ScatShape<S>::NT)
+    k_scatter_blocks_df(const double* __restrict__ vis5, const int32_t* __restrict__ order,
+                        const int32_t* __restrict__ offs, int nkeys, int nbx,
+                        const double2* __restrict__ gcf, const float4* __restrict__ gcf_df,
+                        const int* __restrict__ exps, double2* __restrict__ grid, SingleGeo geo) {
+  using Z = ScatShape<S>;
+  extern __shared__ __align__(16) unsigned char smem[];
+  float4* acc = (float4*)smem;
+  ScatRec* srec = (ScatRec*)(acc + Z::RA * Z::As);
+  const int64_t n_kept = offs[nkeys - 1];  // the records without a kept footprint come last
+  const int64_t c0 = (int64_t)blockIdx.x * Z::CH;
+  if (c0 >= n_kept) return;
+  const int64_t c1 = min(n_kept, c0 + Z::CH);
+  const int t = threadIdx.x;
+  if (exps[0] == kExpNonFinite || exps[1] == kExpNonFinite) {
+    const int lane = t & 31;
+    for (int64_t k = c0 + (t >> 5); k < c1; k += Z::NT / 32) {
+      const double* r = vis5 + 5 * (int64_t)order[k];
+      const VisIndex ix = vis_index(r[0], r[1], geo.scale, geo.grid_size, S, geo.margin,
+                                    geo.min_x, geo.min_y, geo.ext_x, geo.ext_y);
+      warp_scatter64(grid + (int64_t)(ix.y0 - geo.min_y) * geo.pitch + (ix.x0 - geo.min_x),
+                     geo.pitch, gcf + (int64_t)ix.phase * S * S, S, r[3], r[4], lane);
+    }
+    return;
+  }
+  const int kv = df_scale_exp(exps[0]);
+  const int kt = kv + df_scale_exp(exps[1]);
+  for (int q = t; q < Z::RA * Z::As; q += Z::NT) acc[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+  const int ra = t % S, rb0 = t / S;
+  int cur = -1;                        // the segment's block
+  int xlo = 0, ylo = 0, xhi = 0, yhi = 0;  // its footprint corners' bounds
+  // the segment's pixels into the grid, and the region cleared
+  auto flush = [&]() {
+    __syncthreads();  // every tap of the segment is in
+    const int ox = (cur % nbx) * kBlk, oy = (cur / nbx) * kBlk;
+    const int w = xhi - xlo + S, h = yhi - ylo + S;
+    for (int q = t; q < w * h; q += Z::NT) {
+      const int yy = ylo + q / w, xx = xlo + q % w;
+      float4* a = acc + yy * Z::As + xx;
+      const float4 v = *a;
+      if (v.x != 0.f || v.y != 0.f || v.z != 0.f || v.w != 0.f) {
+        const int gx = ox + xx, gy = oy + yy;
+        if (gx < geo.ext_x && gy < geo.ext_y) {
+          double2* p = grid + (int64_t)gy * geo.pitch + gx;
+          const double2 d = df_to_double(v, kt);
+          atomicAdd(&p->x, d.x);
+          atomicAdd(&p->y, d.y);
+        }
+        *a = make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+    }
+    __syncthreads();  // cleared before the next segment's taps
+  };
+  for (int64_t b = c0; b < c1; b += Z::NT) {
+    const int nb = (int)min((int64_t)Z::NT, c1 - b);
+    __syncthreads();  // the previous batch is consumed
+    if (t < nb) {
+      const double* r = vis5 + 5 * (int64_t)order[b + t];
+      const VisIndex ix = vis_index(r[0], r[1], geo.scale, geo.grid_size, S, geo.margin,
+                                    geo.min_x, geo.min_y, geo.ext_x, geo.ext_y);
+      const int x = ix.x0 - geo.min_x, y = ix.y0 - geo.min_y;
+      ScatRec d;
+      d.key = (y / kBlk) * nbx + x / kBlk;
+      d.x0 = x % kBlk;
+      d.y0 = y % kBlk;
+      d.phase = ix.phase;
+      const float2 re = df_split((unsigned long long)__double_as_longlong(r[3]), kv);
+      const float2 im = df_split((unsigned long long)__double_as_longlong(r[4]), kv);
+      d.vis = make_float4(re.x, re.y, im.x, im.y);
+      srec[t] = d;
+    }
+    __syncthreads();
+    for (int k = 0; k < nb; k++) {
+      const ScatRec d = srec[k];  // the same record for every thread
+      if (d.key != cur) {
+        if (cur >= 0) flush();
+        cur = d.key;
+        xlo = xhi = d.x0;
+        ylo = yhi = d.y0;
+      } else {
+        xlo = min(xlo, d.x0);
+        xhi = max(xhi, d.x0);
+        ylo = min(ylo, d.y0);
+        yhi = max(yhi, d.y0);
+      }
+      const int i = (ra - d.x0) & (S - 1), ym = d.y0;
+      const float4* g = gcf_df + (int64_t)d.phase * S * S + i;
+      float4* a = acc + d.y0 * Z::As + d.x0 + i;
+#pragma unroll 4
+      for (int m = 0; m < Z::R; m++) {
+        const int j = (rb0 + m * Z::DR - ym) & (S - 1);
+        const float4 c = __ldg(g + j * S);
+        float4 v = a[j * Z::As];
+        df_cmac<false>(d.vis, c, v);
+        a[j * Z::As] = v;
+      }
+    }
+  }
+  if (cur >= 0) flush();
+}
+
+// Gridding of a call's n device records into the device grid `grid` (W x H,
+// rows W apart; zero, or zero on the blocks the records touch): the
+// shared-memory double-float kernel for GCF sizes 16, 32 and 64, the warp
+// kernel with FP64 atomics otherwise.  Staging slots 5 (GCF split, exponents),
+// 7 and 8 (the records' order).
+static int scatter_records(int64_t n, const void* d_vis, const void* d_gcf, double2* grid,
+                           const SingleGeo& geo, const int32_t* order, cudaStream_t s) {
+  const int S = geo.S;
+  int rc;
+  if (!order && (rc = order_by_block(n, d_vis, geo, (int32_t**)&order, s))) return rc;
+  if (S != 16 && S != 32 && S != 64) {
+    int blocks;
+    const int threads = plain_grid_dims(n, &blocks);
+    k_scatter_single64<<<blocks, threads, 0, s>>>(n, (const double*)d_vis,
+                                                  (const double2*)d_gcf, grid, geo, order);
+    GB_CUDA_TRY(cudaGetLastError());
+    return GB_OK;
+  }
+  const int64_t n_gcf = (int64_t)GB_PHASES * S * S;
+  void* d_df;
+  if ((rc = stage_buffer(5, (size_t)n_gcf * 16 + 16, &d_df))) return rc;
+  float4* gcf_df = (float4*)d_df;
+  int* exps = (int*)((char*)d_df + (size_t)n_gcf * 16);
+  // exps[0]: the visibilities' (fields 3 and 4 of each record), exps[1]: the GCF's
+  GB_CUDA_TRY(cudaMemsetAsync(exps, 0, 2 * sizeof(int), s));
+  const int vb = (int)std::clamp<int64_t>((n + 255) / 256, 1, 4096);
+  const dim3 gc((unsigned)std::clamp<int64_t>((2 * n_gcf + 255) / 256, 1, (int64_t)sm_count() * 4),
+                1);
+  k_max_exponent<<<dim3(1, vb), 32, 0, s>>>((const double*)d_vis + 3, n, 2, 5, exps);
+  k_max_exponent<<<gc, 256, 0, s>>>((const double*)d_gcf, 1, 2 * n_gcf, 2 * n_gcf, exps + 1);
+  k_df_split<<<gc, 256, 0, s>>>((const double*)d_gcf, 1, 2 * n_gcf, 2 * n_gcf, exps, 1,
+                                (float2*)gcf_df);
+  GB_CUDA_TRY(cudaGetLastError());
+  const int nbx = (geo.ext_x + kBlk - 1) / kBlk, nby = (geo.ext_y + kBlk - 1) / kBlk;
+  const int nkeys = nbx * nby + 1;
+  // order_by_block keeps (hist, offs, cursor) in slot 7
+  void* d_keys;
+  if ((rc = stage_buffer(7, (size_t)3 * nkeys * sizeof(int32_t), &d_keys))) return rc;
+  const int32_t* offs = (const int32_t*)d_keys + nkeys;
+  static std::once_flag attr[3];
+  auto launch = [&](auto tag) -> int {
+    constexpr int SS = decltype(tag)::value;
+    using Z = ScatShape<SS>;
+    std::call_once(attr[SS == 16 ? 0 : SS == 32 ? 1 : 2], [] {
+      cudaFuncSetAttribute(k_scatter_blocks_df<SS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)scatter_blocks_smem<SS>());
+    });
+    const int64_t chunks = (n + Z::CH - 1) / Z::CH;
+    k_scatter_blocks_df<SS><<<(unsigned)chunks, Z::NT, scatter_blocks_smem<SS>(), s>>>(
+        (const double*)d_vis, order, offs, nkeys, nbx, (const double2*)d_gcf, gcf_df, exps, grid,
+        geo);
+    GB_CUDA_TRY(cudaGetLastError());
+    return GB_OK;
+  };
+  return S == 16   ? launch(std::integral_constant<int, 16>{})
+         : S == 32 ? launch(std::integral_constant<int, 32>{})
+                   : launch(std::integral_constant<int, 64>{});
+}
+
 int df_reserve(DfScratch& d, int64_t grid_elems, int64_t gcf_elems) {
   int rc;
   if (!d.exps && (rc = dev_alloc((void**)&d.exps, 2 * sizeof(int), "FP64 degrid scratch")))
@@ -807,10 +1007,10 @@ static int compat_scatter(const char* who, int size_err, double scale, int32_t g
         (rc = order_by_block(n, d_vis, geo, &order, s)))
       return rc;
     k_zero_marked<<<nbx * nby, 256, 0, s>>>((double2*)d_acc, W, H, nbx, marks);
-    int blocks;
-    const int threads = plain_grid_dims(n, &blocks);
-    k_scatter_single64<<<blocks, threads, 0, s>>>(n, (const double*)d_vis, (const double2*)d_gcf,
-                                                  (double2*)d_acc, geo, order);
+    if ((rc = scatter_records(n, d_vis, d_gcf, (double2*)d_acc, geo, order, s))) {
+      cudaStreamSynchronize(s);
+      return rc;
+    }
     k_flush_host<<<nbx * nby, 256, 0, s>>>((double*)uvg->host, row, (const double2*)d_acc, W, H,
                                            nbx, marks);
     GB_CUDA_TRY(cudaGetLastError());
@@ -836,11 +1036,11 @@ static int compat_scatter(const char* who, int size_err, double scale, int32_t g
   GB_CUDA_TRY(cudaEventRecord(ev, s));
   GB_CUDA_TRY(cudaStreamWaitEvent(s2, ev, 0));
   SingleGeo geo{scale, grid_size, margin, S, uvg->min[1], uvg->min[2], W, H, (int64_t)W};
-  int blocks;
-  const int threads = plain_grid_dims(n, &blocks);
-  k_scatter_single64<<<blocks, threads, 0, s2>>>(n, (const double*)d_vis, (const double2*)d_gcf,
-                                                 (double2*)d_acc, geo, nullptr);
-  GB_TRY_DRAIN(cudaGetLastError(), s, s2);
+  if ((rc = scatter_records(n, d_vis, d_gcf, (double2*)d_acc, geo, nullptr, s2))) {
+    cudaStreamSynchronize(s);
+    cudaStreamSynchronize(s2);
+    return rc;
+  }
   GB_TRY_DRAIN(cudaEventRecord(ev, s2), s, s2);
   GB_TRY_DRAIN(cudaMemcpy2DAsync(d_grid, (size_t)W * 16, uvg->host, (size_t)row * 8,
                                  (size_t)W * 16, H, cudaMemcpyHostToDevice, s),

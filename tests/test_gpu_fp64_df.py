@@ -132,3 +132,65 @@ def test_reference_abi_with_nan_and_extreme_scales():
     assert compat.call_degrid("kern_degrid_gpu1", 1.0, G, S, gcf, grid, vis5, out) == 0
     exp = O.degrid(1.0, G, S, gcf, grid, vis5)
     _same_nonfinite(out[:, 3], exp[:, 3])
+
+
+def _scatter_case(seed, S, n=3000, G=256):
+    rng = np.random.default_rng(seed)
+    vis5 = np.zeros((n, 5))
+    vis5[:, :2] = rng.uniform(-0.45 * G, 0.45 * G, (n, 2))
+    vis5[:, 3:] = rng.standard_normal((n, 2))
+    vis5[:40, 0] = 1e9  # out of bounds
+    gcf = rng.standard_normal((64, S, S)) + 1j * rng.standard_normal((64, S, S))
+    return vis5, gcf, G
+
+
+def _abi_scatter(vis5, gcf, G, margin=64):
+    # a zero grid: the increments span magnitudes a unit grid would absorb
+    got = np.zeros((G, G), np.complex128)
+    assert compat.call_scatter("kern_scatter_gpu1", 1.0, G, margin, vis5, gcf, got) == 0
+    exp = np.zeros_like(got)
+    O.scatter(1.0, G, margin, vis5, gcf, exp)
+    return got, exp
+
+
+@pytest.mark.parametrize("S", [16, 32, 64])
+@pytest.mark.parametrize("sv,sc", [(1e150, 1e-200), (2.0 ** -1000, 1.0), (1e-300, 1e300)])
+def test_reference_abi_scatter_extreme_magnitudes(S, sv, sc):
+    """The shared-memory double-float gridder behind kern_scatter_gpu1 (GCF
+    sizes 16, 32, 64) with visibilities and GCFs scaled far apart."""
+    vis5, gcf, G = _scatter_case(60 + S, S)
+    vis5[:, 3:] *= sv
+    got, exp = _abi_scatter(vis5, gcf * sc, G)
+    assert np.isfinite(exp).all() and np.abs(exp).max() > 0
+    assert rel_l2(got, exp) < TOL64
+
+
+@pytest.mark.parametrize("S", [16, 64])
+def test_reference_abi_scatter_forty_decades(S):
+    vis5, gcf, G = _scatter_case(70 + S, S)
+    rng = np.random.default_rng(3)
+    vis5[:, 3:] *= 10.0 ** rng.uniform(-40, 0, (len(vis5), 1))
+    gcf[rng.uniform(0, 1, gcf.shape) < 0.2] = 0
+    got, exp = _abi_scatter(vis5, gcf, G)
+    assert rel_l2(got, exp) < TOL64
+
+
+@pytest.mark.parametrize("S", [16, 32, 64])
+def test_reference_abi_scatter_nonfinite_and_subnormal(S):
+    """A NaN visibility or an Inf GCF tap sends the call down the FP64
+    atomics, which propagate them as the oracle does; so does a subnormal."""
+    vis5, gcf, G = _scatter_case(80 + S, S)
+    v = vis5.copy()
+    v[500, :2] = 0.0  # a kept footprint at the centre
+    v[500, 3] = np.nan
+    got, exp = _abi_scatter(v, gcf, G)
+    _same_nonfinite(got, exp)
+    g = gcf.copy()
+    g[5, 3, 2] = np.inf
+    got, exp = _abi_scatter(vis5, g, G)
+    _same_nonfinite(got, exp)
+    v = vis5.copy()
+    v[:, 3:] *= 1e-310
+    got, exp = _abi_scatter(v, gcf, G)
+    assert np.abs(exp).max() > 0
+    assert np.abs(got - exp).max() < 1e-318 * 4 * S * S
