@@ -195,30 +195,73 @@ __device__ __forceinline__ void df_cmac(const float4 a, float4 b, float4& acc) {
 }
 
 // The footprint's double-float sum over a group of L lanes (an aligned part
-// of the warp, `mask` its lanes; lane = the lane's index in the group).
+// of the warp, `mask` its lanes; lane = the lane's index in the group).  A
+// lane takes its taps four at a time, all eight loads issued first, into four
+// running sums (four independent addition chains), which are added at the end.
 template <bool CONJ, int L = 32>
 __device__ __forceinline__ float4 warp_gather_df(const float4* __restrict__ base, int64_t pitch,
                                                  const float4* __restrict__ g, int S, int lane,
                                                  unsigned mask = 0xffffffffu) {
-  float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+  constexpr int U = 4;
+  float4 acc[U];
+#pragma unroll
+  for (int u = 0; u < U; u++) acc[u] = make_float4(0.f, 0.f, 0.f, 0.f);
   TapWalk w(S, lane, L);
-  for (; w.j < S; w.next())
-    df_cmac<CONJ>(base[(int64_t)w.j * pitch + w.i], __ldg(g + w.j * S + w.i), acc);
+  while (w.j < S) {
+    int64_t ob[U];
+    int og[U];
+    bool ok[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      ok[u] = w.j < S;
+      ob[u] = ok[u] ? (int64_t)w.j * pitch + w.i : 0;
+      og[u] = ok[u] ? w.j * S + w.i : 0;
+      w.next();
+    }
+    float4 x[U], c[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      x[u] = ok[u] ? base[ob[u]] : make_float4(0.f, 0.f, 0.f, 0.f);
+      c[u] = ok[u] ? __ldg(g + og[u]) : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+#pragma unroll
+    for (int u = 0; u < U; u++) df_cmac<CONJ>(x[u], c[u], acc[u]);
+  }
+#pragma unroll
+  for (int u = 1; u < U; u++) {
+    acc[0].z = __fadd_rn(acc[0].z, acc[u].z);
+    acc[0].w = __fadd_rn(acc[0].w, acc[u].w);
+    two_sum_acc(acc[0].x, acc[0].z, acc[u].x);
+    two_sum_acc(acc[0].y, acc[0].w, acc[u].y);
+  }
+  float4 r = acc[0];
 #pragma unroll
   for (int o = L / 2; o > 0; o >>= 1) {
-    const float sr = __shfl_xor_sync(mask, acc.x, o);
-    const float si = __shfl_xor_sync(mask, acc.y, o);
-    acc.z = __fadd_rn(acc.z, __shfl_xor_sync(mask, acc.z, o));
-    acc.w = __fadd_rn(acc.w, __shfl_xor_sync(mask, acc.w, o));
-    two_sum_acc(acc.x, acc.z, sr);
-    two_sum_acc(acc.y, acc.w, si);
+    const float sr = __shfl_xor_sync(mask, r.x, o);
+    const float si = __shfl_xor_sync(mask, r.y, o);
+    r.z = __fadd_rn(r.z, __shfl_xor_sync(mask, r.z, o));
+    r.w = __fadd_rn(r.w, __shfl_xor_sync(mask, r.w, o));
+    two_sum_acc(r.x, r.z, sr);
+    two_sum_acc(r.y, r.w, si);
   }
-  return acc;
+  return r;
 }
 
 // A double-float sum back to FP64, times 2^kt.
 __device__ __forceinline__ double2 df_to_double(float4 a, int kt) {
   return make_double2(ldexp((double)a.x + (double)a.z, kt), ldexp((double)a.y + (double)a.w, kt));
+}
+
+// 2^kt as a double when it is a normal number (else 0: use df_to_double).
+__device__ __forceinline__ double df_pow2(int kt) {
+  return kt > -1023 && kt < 1024 ? __longlong_as_double((long long)(kt + 1023) << 52) : 0.0;
+}
+
+// df_to_double with the factor 2^kt given as sc = df_pow2(kt) (one multiply
+// instead of ldexp's range handling; the same result while sc is normal).
+__device__ __forceinline__ double2 df_to_double_sc(float4 a, int kt, double sc) {
+  if (sc == 0.0) return df_to_double(a, kt);
+  return make_double2(((double)a.x + (double)a.z) * sc, ((double)a.y + (double)a.w) * sc);
 }
 
 // Lane l of a warp indexes visibility t0 + l once; the warp then takes the
@@ -295,17 +338,17 @@ __global__ void k_degrid_single64(int64_t n, const double* __restrict__ vis5,
                                   const float4* __restrict__ gcf_df,
                                   const float4* __restrict__ grid_df,
                                   const int* __restrict__ exps, double* __restrict__ out5,
-                                  SingleGeo geo, const int32_t* __restrict__ order) {
+                                  SingleGeo geo, const int32_t* __restrict__ order, int pw) {
   const int lane = threadIdx.x & 31;
   const bool df = exps[0] != kExpNonFinite && exps[1] != kExpNonFinite;
   const int kt = df_scale_exp(exps[0]) + df_scale_exp(exps[1]);
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
-  for (int64_t t0 = 32 * (blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5)); t0 < n;
-       t0 += 32 * warps) {
-    const bool mine_ok = t0 + lane < n;
+  for (int64_t t0 = pw * (blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5)); t0 < n;
+       t0 += pw * warps) {
+    const int m = (int)min((int64_t)pw, n - t0);
+    const bool mine_ok = lane < m;
     const int64_t t = visit_rec(order, t0 + lane, n);
-    const LaneIndex mine = single_index(vis5, t, n, geo);
-    const int m = (int)min((int64_t)32, n - t0);
+    const LaneIndex mine = single_index(vis5, mine_ok ? t : n, n, geo);
     float4 acc_df = make_float4(0.f, 0.f, 0.f, 0.f);
     double2 acc = make_double2(0.0, 0.0);
     if (df && geo.S <= 8) {
@@ -446,6 +489,16 @@ __global__ void k_degrid_plain64(PlanDev P, const double2* __restrict__ gcf,
   }
 }
 
+// Launch shape of k_degrid_single64: pw records per warp (32, fewer for a
+// call too small to occupy every SM with 32 warps), 8 warps per block.
+static int single_degrid_dims(int64_t n, int* blocks, int* pw) {
+  const int64_t target = (int64_t)sm_count() * 32;
+  *pw = (int)std::clamp<int64_t>((n + target - 1) / target, 1, 32);
+  const int64_t warps = (n + *pw - 1) / *pw;
+  *blocks = (int)std::clamp<int64_t>((warps + 7) / 8, 1, (int64_t)sm_count() * 8);
+  return 256;
+}
+
 static int plain_grid_dims(int64_t n, int* blocks) {
   const int64_t warps_needed = (n + 31) / 32;
   int64_t b = (warps_needed + 7) / 8;
@@ -528,19 +581,51 @@ __global__ void k_flush_host(double* __restrict__ host, int64_t row,
   }
 }
 
-// d = the host grid on the marked blocks, 0 on the others (every block written)
+// d = the host grid on the marked blocks (the other blocks are not written:
+// nothing reads them), and *exp max-ed with the largest exponent field of
+// what was read (k_max_exponent's rule)
 __global__ void k_gather_host(double2* __restrict__ d, const double* __restrict__ host,
                               int64_t row, int W, int H, int nbx,
-                              const unsigned char* __restrict__ marks) {
+                              const unsigned char* __restrict__ marks, int* __restrict__ exp) {
   const int b = blockIdx.x;
-  const bool on = marks[b] != 0;
+  if (!marks[b]) return;
+  const int bx = b % nbx, by = b / nbx;
+  int m = 0;
+  for (int k = threadIdx.x; k < kBlk * kBlk; k += blockDim.x) {
+    const int x = bx * kBlk + (k % kBlk), y = by * kBlk + k / kBlk;
+    if (x < W && y < H) {
+      const double2 v = *(reinterpret_cast<const double2*>(host + (int64_t)y * row) + x);
+      d[(int64_t)y * W + x] = v;
+      const unsigned long long bits[2] = {(unsigned long long)__double_as_longlong(v.x),
+                                          (unsigned long long)__double_as_longlong(v.y)};
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        const int e = (int)((bits[h] >> 52) & 0x7FF);
+        m = max(m, e == 0 && (bits[h] & 0xFFFFFFFFFFFFFull) ? kExpNonFinite : e);
+      }
+    }
+  }
+  m = __reduce_max_sync(0xffffffffu, m);
+  if ((threadIdx.x & 31) == 0 && m) atomicMax(exp, m);
+}
+
+// The double-float split of d (W x H, rows W apart) on the marked blocks,
+// under the scale of exps[0] (nothing when either exponent is non-finite).
+__global__ void k_df_split_marked(const double2* __restrict__ d, int W, int H, int nbx,
+                                  const unsigned char* __restrict__ marks,
+                                  const int* __restrict__ exps, float4* __restrict__ out) {
+  const int b = blockIdx.x;
+  if (!marks[b] || exps[0] == kExpNonFinite || exps[1] == kExpNonFinite) return;
+  const int k0 = df_scale_exp(exps[0]);
   const int bx = b % nbx, by = b / nbx;
   for (int k = threadIdx.x; k < kBlk * kBlk; k += blockDim.x) {
     const int x = bx * kBlk + (k % kBlk), y = by * kBlk + k / kBlk;
-    if (x < W && y < H)
-      d[(int64_t)y * W + x] =
-          on ? *(reinterpret_cast<const double2*>(host + (int64_t)y * row) + x)
-             : make_double2(0.0, 0.0);
+    if (x < W && y < H) {
+      const double2 v = d[(int64_t)y * W + x];
+      const float2 re = df_split((unsigned long long)__double_as_longlong(v.x), k0);
+      const float2 im = df_split((unsigned long long)__double_as_longlong(v.y), k0);
+      out[(int64_t)y * W + x] = make_float4(re.x, re.y, im.x, im.y);
+    }
   }
 }
 
@@ -652,7 +737,7 @@ static int df_prepare(const double* grid, int32_t ext_x, int32_t ext_y, int64_t 
 // kern_scatter_gpu1 and its siblings for GCF sizes 16, 32 and 64.  A call's
 // kept records, counting-sorted by the kBlk x kBlk block of their footprint
 // corner (order_by_block), are cut into chunks of ScatShape<S>::CH
-// consecutive records, one CTA per chunk.  A CTA accumulates the records of
+// consecutive records (fewer for a call with few records), one CTA per chunk.  A CTA accumulates the records of
 // one block at a time in shared memory, over the block's footprint region
 // ((kBlk + S - 1)^2 pixels), in the degridders' double-float arithmetic
 // (products and sums err by about 2^-48 of their size); each thread owns the
@@ -668,7 +753,8 @@ struct ScatShape {
   static constexpr int NT = S == 64 ? 512 : 256;  // threads per CTA
   static constexpr int R = S * S / NT;            // residue slots per thread
   static constexpr int DR = NT / S;               // residue rows between a thread's slots
-  static constexpr int CH = S == 16 ? 512 : S == 32 ? 256 : 128;  // records per CTA
+  static constexpr int CH = S == 16 ? 512 : S == 32 ? 256 : 128;  // at most, records per CTA
+  static constexpr int CPS = S == 16 ? 5 : S == 32 ? 3 : 1;       // CTAs per SM (shared memory)
   static constexpr int RA = kBlk + S - 1;         // region edge (pixels)
   static constexpr int As = (RA + 7) & ~7;        // region row stride (float4)
 };
@@ -691,15 +777,16 @@ __global__ void __launch_bounds__(ScatShape<S>::NT)
     k_scatter_blocks_df(const double* __restrict__ vis5, const int32_t* __restrict__ order,
                         const int32_t* __restrict__ offs, int nkeys, int nbx,
                         const double2* __restrict__ gcf, const float4* __restrict__ gcf_df,
-                        const int* __restrict__ exps, double2* __restrict__ grid, SingleGeo geo) {
+                        const int* __restrict__ exps, double2* __restrict__ grid, SingleGeo geo,
+                        int ch) {
   using Z = ScatShape<S>;
   extern __shared__ __align__(16) unsigned char smem[];
   float4* acc = (float4*)smem;
   ScatRec* srec = (ScatRec*)(acc + Z::RA * Z::As);
   const int64_t n_kept = offs[nkeys - 1];  // the records without a kept footprint come last
-  const int64_t c0 = (int64_t)blockIdx.x * Z::CH;
+  const int64_t c0 = (int64_t)blockIdx.x * ch;
   if (c0 >= n_kept) return;
-  const int64_t c1 = min(n_kept, c0 + Z::CH);
+  const int64_t c1 = min(n_kept, c0 + ch);
   const int t = threadIdx.x;
   if (exps[0] == kExpNonFinite || exps[1] == kExpNonFinite) {
     const int lane = t & 31;
@@ -714,6 +801,7 @@ __global__ void __launch_bounds__(ScatShape<S>::NT)
   }
   const int kv = df_scale_exp(exps[0]);
   const int kt = kv + df_scale_exp(exps[1]);
+  const double sc = df_pow2(kt);
   for (int q = t; q < Z::RA * Z::As; q += Z::NT) acc[q] = make_float4(0.f, 0.f, 0.f, 0.f);
   const int ra = t % S, rb0 = t / S;
   int cur = -1;                        // the segment's block
@@ -731,7 +819,7 @@ __global__ void __launch_bounds__(ScatShape<S>::NT)
         const int gx = ox + xx, gy = oy + yy;
         if (gx < geo.ext_x && gy < geo.ext_y) {
           double2* p = grid + (int64_t)gy * geo.pitch + gx;
-          const double2 d = df_to_double(v, kt);
+          const double2 d = df_to_double_sc(v, kt, sc);
           atomicAdd(&p->x, d.x);
           atomicAdd(&p->y, d.y);
         }
@@ -835,10 +923,16 @@ static int scatter_records(int64_t n, const void* d_vis, const void* d_gcf, doub
       cudaFuncSetAttribute(k_scatter_blocks_df<SS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)scatter_blocks_smem<SS>());
     });
-    const int64_t chunks = (n + Z::CH - 1) / Z::CH;
+    // chunks of up to CH records, smaller for a call too small to give every
+    // SM two CTAs' worth (sparse w-bins: their records mostly have a block
+    // each, and a CTA then grids one or a few)
+    const int64_t ch = std::clamp<int64_t>((n + 2 * Z::CPS * sm_count() - 1) /
+                                               (2 * Z::CPS * (int64_t)sm_count()),
+                                           1, Z::CH);
+    const int64_t chunks = (n + ch - 1) / ch;
     k_scatter_blocks_df<SS><<<(unsigned)chunks, Z::NT, scatter_blocks_smem<SS>(), s>>>(
         (const double*)d_vis, order, offs, nkeys, nbx, (const double2*)d_gcf, gcf_df, exps, grid,
-        geo);
+        geo, (int)ch);
     GB_CUDA_TRY(cudaGetLastError());
     return GB_OK;
   };
@@ -1107,27 +1201,40 @@ static int compat_degrid(const char* who, int size_err, double scale, int32_t gr
     if ((rc = stage_buffer(6, (size_t)nbx * nby, &d_marks))) return rc;
     unsigned char* marks = (unsigned char*)d_marks;
     if ((rc = mark_blocks(n, d_vis, geo, nbx, nby, marks, s))) return rc;
+    // the grid's blocks gathered with their exponent, then split; the GCF's
+    // exponent and split as df_prepare makes them
+    const int64_t n_gcf = (int64_t)GB_PHASES * S * S;
+    const dim3 gc((unsigned)std::clamp<int64_t>((2 * n_gcf + 255) / 256, 1,
+                                                (int64_t)sm_count() * 4),
+                  1);
+    GB_CUDA_TRY(cudaMemsetAsync(d_exps, 0, 2 * sizeof(int), s));
     k_gather_host<<<nbx * nby, 256, 0, s>>>((double2*)d_grid, (const double*)uvg->host, row, W, H,
-                                            nbx, marks);
+                                            nbx, marks, d_exps);
+    k_max_exponent<<<gc, 256, 0, s>>>((const double*)d_gcf, 1, 2 * n_gcf, 2 * n_gcf, d_exps + 1);
+    k_df_split_marked<<<nbx * nby, 256, 0, s>>>((const double2*)d_grid, W, H, nbx, marks, d_exps,
+                                                (float4*)d_grid_df);
+    k_df_split<<<gc, 256, 0, s>>>((const double*)d_gcf, 1, 2 * n_gcf, 2 * n_gcf, d_exps, 1,
+                                  (float2*)d_gcf_df);
     GB_CUDA_TRY(cudaGetLastError());
   } else {
     GB_CUDA_TRY(cudaMemcpy2DAsync(d_grid, (size_t)W * 16, uvg->host, (size_t)row * 8,
                                   (size_t)W * 16, H, cudaMemcpyHostToDevice, s));
+    if ((rc = df_prepare((const double*)d_grid, W, H, W, (const double*)d_gcf,
+                         (int64_t)GB_PHASES * S * S, (float4*)d_grid_df, (float4*)d_gcf_df,
+                         d_exps, s)))
+      return rc;
   }
-  if ((rc = df_prepare((const double*)d_grid, W, H, W, (const double*)d_gcf,
-                       (int64_t)GB_PHASES * S * S, (float4*)d_grid_df, (float4*)d_gcf_df, d_exps,
-                       s)))
-    return rc;
   if (direct) {
     // one launch over the records in grid-block order (neighbouring warps
     // gather from the same grid lines), then one download of the results
     int32_t* order = nullptr;
     if ((rc = order_by_block(n, d_vis, geo, &order, s))) return rc;
-    int blocks;
-    const int threads = plain_grid_dims(n, &blocks);
+    int blocks, pw;
+    const int threads = single_degrid_dims(n, &blocks, &pw);
     k_degrid_single64<<<blocks, threads, 0, s>>>(
         n, (const double*)d_vis, (const double2*)d_gcf, (const double2*)d_grid,
-        (const float4*)d_gcf_df, (const float4*)d_grid_df, d_exps, (double*)d_out, geo, order);
+        (const float4*)d_gcf_df, (const float4*)d_grid_df, d_exps, (double*)d_out, geo, order,
+        pw);
     GB_CUDA_TRY(cudaGetLastError());
     GB_CUDA_TRY(cudaMemcpyAsync(vis_out->host, d_out, (size_t)n * 40, cudaMemcpyDeviceToHost, s));
     GB_CUDA_TRY(cudaStreamSynchronize(s));
@@ -1144,12 +1251,12 @@ static int compat_degrid(const char* who, int size_err, double scale, int32_t gr
   const int chunks = n >= (1 << 18) ? kAuxEvents : 1;
   for (int c = 0; c < chunks; c++) {
     const int64_t c0 = n * c / chunks, c1 = n * (c + 1) / chunks;
-    int blocks;
-    const int threads = plain_grid_dims(c1 - c0, &blocks);
+    int blocks, pw;
+    const int threads = single_degrid_dims(c1 - c0, &blocks, &pw);
     k_degrid_single64<<<blocks, threads, 0, s>>>(
         c1 - c0, (const double*)d_vis + 5 * c0, (const double2*)d_gcf, (const double2*)d_grid,
         (const float4*)d_gcf_df, (const float4*)d_grid_df, d_exps, (double*)d_out + 5 * c0, geo,
-        nullptr);
+        nullptr, pw);
     GB_TRY_DRAIN(cudaGetLastError(), s, s2);
     GB_TRY_DRAIN(cudaEventRecord(evs[c], s), s, s2);
   }
