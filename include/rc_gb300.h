@@ -77,7 +77,13 @@ const char *gb_version(void);
  * The reference dispatchers accept S in {8, 16, 32, 64} and return the legacy
  * code otherwise; these do the same (the engine below accepts any S). */
 
-/* replaces MS6/kernel/gpu/gridding/kern_scatter_gpu1.cpp:21-40 */
+/* Precision of the gridders (kern_scatter_gpu1, kern_scatter, nvGridder):
+ * for GCF sizes 16, 32 and 64 the taps are summed per 32 x 32 grid block in
+ * shared memory in the degridders' double-float arithmetic (below), and each
+ * block's sums are added into the grid with FP64 atomics; size 8 adds FP64
+ * products with FP64 atomics.  Either way the addition order varies between
+ * runs.  Inputs holding an Inf, a NaN or a subnormal take the FP64 atomics.
+ * replaces MS6/kernel/gpu/gridding/kern_scatter_gpu1.cpp:21-40 */
 int kern_scatter_gpu1(double scale, int32_t grid_size, int32_t margin_size,
                       buffer_t *vis, buffer_t *gcf, buffer_t *uvg);
 #ifndef GB_MS5_ABI /* the MS5 variant binds its own kern_scatter (rc_gb300_ms5.h) */

@@ -1,15 +1,17 @@
 // Plain FP64 gridder / degridder (complex128) and the reference-ABI entry
 // points built on them.
 //
-// "Plain" = no sorting, no tiling, no shared memory: one warp per
-// visibility, lanes over the S*S taps, FP64 atomics into the grid (gridding)
-// or a warp-shuffle reduction (degridding, computed in double-float; see the
-// section below).  Each lane computes the FP64 index math of one of 32
-// visibilities and the warp takes them in turn.  It is the FP64 GPU comparison
-// path of the engine and the implementation behind kern_scatter_gpu1 /
-// kern_degrid_gpu1 / nvGridder / kern_scatter / kern_degrid, whose semantics
-// are the reference's (MS6/kernel/cpu/gridding/scatter.cpp:56-111,
-// degrid.cpp:41-98) on Halide buffer_t host buffers.
+// "Plain" = no tiling: one warp per visibility, lanes over the S*S taps,
+// FP64 atomics into the grid (gridding) or a warp-shuffle reduction
+// (degridding, computed in double-float; see the section below).  Each lane
+// computes the FP64 index math of one of up to 32 visibilities and the warp
+// takes them in turn.  It is the FP64 GPU comparison path of the engine and
+// the implementation behind kern_degrid_gpu1 / kern_degrid, and behind
+// kern_scatter_gpu1 / nvGridder / kern_scatter for GCF size 8; for sizes 16,
+// 32 and 64 those gridders sum each 32 x 32 grid block's taps in shared memory
+// in double-float first (k_scatter_blocks_df).  Semantics are the reference's
+// (MS6/kernel/cpu/gridding/scatter.cpp:56-111, degrid.cpp:41-98) on Halide
+// buffer_t host buffers.
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -750,7 +752,7 @@ static int df_prepare(const double* grid, int32_t ext_x, int32_t ext_y, int64_t 
 // atomics of warp_scatter64 instead, so that those propagate as FP64 would.
 template <int S>
 struct ScatShape {
-  static constexpr int NT = S == 64 ? 512 : 256;  // threads per CTA
+  static constexpr int NT = S == 64 ? 1024 : 256;  // threads per CTA
   static constexpr int R = S * S / NT;            // residue slots per thread
   static constexpr int DR = NT / S;               // residue rows between a thread's slots
   static constexpr int CH = S == 16 ? 512 : S == 32 ? 256 : 128;  // at most, records per CTA
