@@ -79,18 +79,18 @@ struct ClassInfo {
   int32_t L, G, A, pmax;
 };
 
-// Shared memory of one thread group: the A x A accumulator (float4: sum and
-// Kahan compensation) or grid stage (float2), plus one batch of L decoded
-// records (32 B each; a gridding record carries its visibility).
-// Gridding accumulator rows are padded to a multiple of 8 pixels (8 float4 =
+// Shared memory of one thread group: the A x A accumulator or grid stage
+// (float2 per pixel), plus one batch of L decoded records (32 B each; a
+// gridding record carries its visibility).
+// Gridding accumulator rows are padded to a multiple of 16 pixels (16 float2 =
 // the 32 shared-memory banks): a warp's read-modify-write that steps to the
 // next pixel row then stays on the banks of a continuing row.
-__host__ __device__ inline int acc_stride(int A) { return (A + 7) & ~7; }
+__host__ __device__ inline int acc_stride(int A) { return (A + 15) & ~15; }
 // (and each record's shape word again, 4 bytes, in an array of its own: the
 // run detection reads 32 consecutive shapes at once, which at the records'
 // 32-byte stride would fall on 4 banks)
 __host__ __device__ inline size_t grid_group_bytes(int A, int L) {
-  return 16 * (size_t)A * acc_stride(A) + 36 * (size_t)L;
+  return 8 * (size_t)A * acc_stride(A) + 36 * (size_t)L;
 }
 // The float2 grid stage is padded to 16 bytes so that the 16-byte records
 // behind it (and the next group's region) stay 16-byte aligned.
