@@ -147,7 +147,7 @@ static int batch_build(gb_batch* B, int32_t n, const gb_batch_member* m, cudaStr
   for (int c = 0; c < B->n_classes; c++) {
     ClassInfo& ci = B->cls[c];
     ci.A = B->T + ci.pmax - 1;
-    const size_t per_group = grid_group_bytes(ci.A, ci.L);
+    const size_t per_group = group_bytes(ci.A, ci.L);
     int G = B->NT / ci.L;
     while (G > 0 && (size_t)G * per_group > (size_t)smem_cap) G--;
     if (G == 0) {

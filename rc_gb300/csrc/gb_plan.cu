@@ -330,7 +330,7 @@ static int build_plan(gb_plan* P, const gb_geometry* geo, int64_t n_vis, const d
     for (int r = 0; r < nper; r++)
       if (rank_cls[r] == c) ci.pmax = std::max(ci.pmax, periods[r]);
     ci.A = P->T + ci.pmax - 1;
-    const size_t per_group = grid_group_bytes(ci.A, ci.L);
+    const size_t per_group = group_bytes(ci.A, ci.L);
     int G = P->NT / ci.L;
     while (G > 0 && (size_t)G * per_group > (size_t)smem_cap) G--;
     if (G == 0) {

@@ -121,6 +121,12 @@ __host__ __device__ inline int16_t item_cls_with_residue(int16_t cls, int split_
 __host__ __device__ inline size_t degrid_group_bytes(int A, int L) {
   return degrid_stage_bytes(A) + 32 * (size_t)L;
 }
+// Shared memory of one thread group in either direction: a plan's classes
+// (and their groups per CTA) serve both kernels.
+__host__ __device__ inline size_t group_bytes(int A, int L) {
+  const size_t g = grid_group_bytes(A, L), d = degrid_group_bytes(A, L);
+  return g > d ? g : d;
+}
 
 constexpr int kMaxClasses = 4;
 
