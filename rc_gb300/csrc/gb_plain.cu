@@ -198,13 +198,14 @@ __device__ __forceinline__ void df_cmac(const float4 a, float4 b, float4& acc) {
 
 // The footprint's double-float sum over a group of L lanes (an aligned part
 // of the warp, `mask` its lanes; lane = the lane's index in the group).  A
-// lane takes its taps four at a time, all eight loads issued first, into four
-// running sums (four independent addition chains), which are added at the end.
-template <bool CONJ, int L = 32>
+// lane takes its taps U at a time, all 2U loads issued first, into U running
+// sums (independent addition chains), which are added at the end: U = 4 where
+// few warps share an SM (small reference-ABI calls), 1 where the registers
+// are better spent on resident warps (the engine's FP64 degridder).
+template <bool CONJ, int L = 32, int U = 1>
 __device__ __forceinline__ float4 warp_gather_df(const float4* __restrict__ base, int64_t pitch,
                                                  const float4* __restrict__ g, int S, int lane,
                                                  unsigned mask = 0xffffffffu) {
-  constexpr int U = 4;
   float4 acc[U];
 #pragma unroll
   for (int u = 0; u < U; u++) acc[u] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -362,7 +363,7 @@ __global__ void k_degrid_single64(int64_t n, const double* __restrict__ vis5,
         const LaneIndex ix = mine.from(jv < m ? jv : m - 1);
         float4 a = make_float4(0.f, 0.f, 0.f, 0.f);
         if (jv < m && ix.keep)  // uniform within the group
-          a = warp_gather_df<false, 8>(grid_df + (int64_t)ix.y0 * geo.ext_x + ix.x0, geo.ext_x,
+          a = warp_gather_df<false, 8, 4>(grid_df + (int64_t)ix.y0 * geo.ext_x + ix.x0, geo.ext_x,
                                        gcf_df + (int64_t)ix.phase * geo.S * geo.S, geo.S, gl,
                                        gmask);
         // lane j0 + q takes the sum of group q
@@ -379,7 +380,7 @@ __global__ void k_degrid_single64(int64_t n, const double* __restrict__ vis5,
       if (!ix.keep) continue;
       const int64_t g0 = (int64_t)ix.phase * geo.S * geo.S;
       if (df) {
-        const float4 a = warp_gather_df<false>(grid_df + (int64_t)ix.y0 * geo.ext_x + ix.x0,
+        const float4 a = warp_gather_df<false, 32, 4>(grid_df + (int64_t)ix.y0 * geo.ext_x + ix.x0,
                                                geo.ext_x, gcf_df + g0, geo.S, lane);
         if (lane == j) acc_df = a;
       } else {
