@@ -233,8 +233,10 @@ int gb_plan_export_index(const gb_plan *plan, int32_t *d_out5, void *stream);
  *   D (degridding): pred[v]    = sum_pix grid[pix] * conj(gcf_v[pix - corner_v])
  * D is the exact adjoint of G: <D x, y> = <x, G y>.  mode 1 of the degridder
  * gives the reference's kern_degrid product instead: pred = -sum grid * gcf.
- * Visibilities the plan skipped get pred = 0.  Per-tile partial sums are
- * compensated (error-free transformation) in shared memory. */
+ * Visibilities the plan skipped get pred = 0.  Gridding sums each tile's
+ * taps in shared memory (float2 per pixel) and adds them into the grid with
+ * float2 atomics; degridding adds each lane's products to a compensated sum.
+ * Against FP64: rel-L2 about 1e-7 to 2e-7 on the benchmark workloads. */
 int gb_grid_f32(gb_plan *plan, const float *d_vis, const float *d_gcf, float *d_grid,
                 void *stream);
 int gb_degrid_f32(gb_plan *plan, const float *d_gcf, const float *d_grid, float *d_pred,
