@@ -210,7 +210,11 @@ __device__ __forceinline__ float4 warp_gather_df(const float4* __restrict__ base
 #pragma unroll
   for (int u = 0; u < U; u++) acc[u] = make_float4(0.f, 0.f, 0.f, 0.f);
   TapWalk w(S, lane, L);
-  while (w.j < S) {
+  if constexpr (U == 1) {
+    for (; w.j < S; w.next())
+      df_cmac<CONJ>(base[(int64_t)w.j * pitch + w.i], __ldg(g + w.j * S + w.i), acc[0]);
+  }
+  while (U > 1 && w.j < S) {
     int64_t ob[U];
     int og[U];
     bool ok[U];
