@@ -115,22 +115,11 @@ struct WBin {
   int64_t count = 0;
 };
 
-// Visibilities: 5-double records u, v, w, re, im (Data.hs:115-123).
-struct Vis {
-  std::vector<double> rec;
-  int64_t size() const { return (int64_t)rec.size() / 5; }
-};
-
-// The visibilities of one (u, v, w-bin) region, zero-padded to its count.
-struct VisBin {
-  WBin bin;
-  Vis vis;
-};
-
 namespace detail {
 // An allocator whose value-initialisation leaves doubles uninitialised: grid
-// buffers are allocated like Flow's (posix_memalign, Flow/Vector.hs:173-190)
-// and zeroed once, by kern_init, not twice.
+// and visibility buffers are allocated like Flow's (posix_memalign,
+// Flow/Vector.hs:173-190); a grid is zeroed once, by kern_init, and a kernel's
+// output records are written whole by the kernel, so neither is zeroed twice.
 template <class T>
 struct NoInit : std::allocator<T> {
   template <class U>
@@ -149,6 +138,19 @@ struct NoInit : std::allocator<T> {
   }
 };
 }  // namespace detail
+
+// Visibilities: 5-double records u, v, w, re, im (Data.hs:115-123).
+struct Vis {
+  std::vector<double, detail::NoInit<double>> rec;
+  int64_t size() const { return (int64_t)rec.size() / 5; }
+};
+
+// The visibilities of one (u, v, w-bin) region, zero-padded to its count.
+struct VisBin {
+  WBin bin;
+  Vis vis;
+};
+
 
 // A complex grid region: dims (2, width, height), strides (1, 2, 2 width),
 // mins (0, min_u, min_v) (Data.hs:64-76, 93-97).
@@ -438,7 +440,7 @@ inline void gridDetiling(UVGrid& tile, UVGrid& full) {
 inline Vis degridKernel(DegridKernelType kt, const GridPar& gp, const GCFPar& gcfp, GCFs& gcf,
                         UVGrid& full, Vis& vis) {
   Vis out;
-  out.rec.assign(vis.rec.size(), 0.0);
+  out.rec.resize(vis.rec.size());  // every record is written by the call
   buffer_t bg = detail::gcf_buffer(gcf), bu = detail::uvg_buffer(full),
            bv = detail::vis_buffer(vis), bo = detail::vis_buffer(out);
   const double scale = gridScale(gp);

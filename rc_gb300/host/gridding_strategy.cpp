@@ -125,6 +125,7 @@ static void time_passes(const std::string& dir, rc::GridKernelType gkt, rc::Degr
   std::vector<double> t_grid, t_degrid;
   rc::UVGrid full;
   std::vector<double> pred_out;
+  pred_out.reserve((size_t)5 * records);
   for (int it = 0; it < warmup + steps; it++) {
     const double t0 = now_ms();
     full = rc::gridInitDetile({0, gp.width}, {0, gp.height});
@@ -203,7 +204,10 @@ int main(int argc, char** argv) {
     const auto dkt = dk == 0 ? rc::DegridKernelType::CPU : rc::DegridKernelType::GPU;
 
     rc::Vis vis;
-    vis.rec = read_doubles(dir + "/vis.bin");
+    {
+      const std::vector<double> v = read_doubles(dir + "/vis.bin");
+      vis.rec.assign(v.begin(), v.end());
+    }
     rc::UVGrid model;
     if (mode == "degrid" || mode == "time") {
       model.width = gp.width;
