@@ -922,11 +922,18 @@ static int scatter_records(int64_t n, const void* d_vis, const void* d_gcf, doub
   void* d_keys;
   if ((rc = stage_buffer(7, (size_t)3 * nkeys * sizeof(int32_t), &d_keys))) return rc;
   const int32_t* offs = (const int32_t*)d_keys + nkeys;
-  static std::once_flag attr[3];
+  // the shared-memory limit of each size's kernel, set once per device
+  static std::once_flag attr[3][64];
+  int dev = 0;
+  GB_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) {
+    gb_set_error(GB_ERR_ARG, "device ordinal %d out of range", dev);
+    return GB_ERR_ARG;
+  }
   auto launch = [&](auto tag) -> int {
     constexpr int SS = decltype(tag)::value;
     using Z = ScatShape<SS>;
-    std::call_once(attr[SS == 16 ? 0 : SS == 32 ? 1 : 2], [] {
+    std::call_once(attr[SS == 16 ? 0 : SS == 32 ? 1 : 2][dev], [] {
       cudaFuncSetAttribute(k_scatter_blocks_df<SS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)scatter_blocks_smem<SS>());
     });
