@@ -78,11 +78,11 @@ const char *gb_version(void);
  * code otherwise; these do the same (the engine below accepts any S). */
 
 /* Precision of the gridders (kern_scatter_gpu1, kern_scatter, nvGridder):
- * for GCF sizes 16, 32 and 64 the taps are summed per 32 x 32 grid block in
- * shared memory in the degridders' double-float arithmetic (below), and each
- * block's sums are added into the grid with FP64 atomics; size 8 adds FP64
- * products with FP64 atomics.  Either way the addition order varies between
- * runs.  Inputs holding an Inf, a NaN or a subnormal take the FP64 atomics.
+ * the taps are summed per 32 x 32 grid block in shared memory in the
+ * degridders' double-float arithmetic (below), and each block's sums are
+ * added into the grid with FP64 atomics, in an order that varies between
+ * runs.  Inputs holding an Inf, a NaN or a subnormal take FP64 products with
+ * FP64 atomics instead.
  * replaces MS6/kernel/gpu/gridding/kern_scatter_gpu1.cpp:21-40 */
 int kern_scatter_gpu1(double scale, int32_t grid_size, int32_t margin_size,
                       buffer_t *vis, buffer_t *gcf, buffer_t *uvg);

@@ -6,12 +6,12 @@
 // (degridding, computed in double-float; see the section below).  Each lane
 // computes the FP64 index math of one of up to 32 visibilities and the warp
 // takes them in turn.  It is the FP64 GPU comparison path of the engine and
-// the implementation behind kern_degrid_gpu1 / kern_degrid, and behind
-// kern_scatter_gpu1 / nvGridder / kern_scatter for GCF size 8; for sizes 16,
-// 32 and 64 those gridders sum each 32 x 32 grid block's taps in shared memory
-// in double-float first (k_scatter_blocks_df).  Semantics are the reference's
-// (MS6/kernel/cpu/gridding/scatter.cpp:56-111, degrid.cpp:41-98) on Halide
-// buffer_t host buffers.
+// the implementation behind kern_degrid_gpu1 / kern_degrid; the gridders
+// kern_scatter_gpu1 / nvGridder / kern_scatter sum each 32 x 32 grid block's
+// taps in shared memory in double-float first (k_scatter_blocks_df) and keep
+// the warp kernel for inputs with an Inf, a NaN or a subnormal.  Semantics
+// are the reference's (MS6/kernel/cpu/gridding/scatter.cpp:56-111,
+// degrid.cpp:41-98) on Halide buffer_t host buffers.
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -741,10 +741,11 @@ static int df_prepare(const double* grid, int32_t ext_x, int32_t ext_y, int64_t 
 }
 
 // ---------------------------------------------------------------- ABI gridding in shared memory
-// kern_scatter_gpu1 and its siblings for GCF sizes 16, 32 and 64.  A call's
-// kept records, counting-sorted by the kBlk x kBlk block of their footprint
-// corner (order_by_block), are cut into chunks of ScatShape<S>::CH
-// consecutive records (fewer for a call with few records), one CTA per chunk.  A CTA accumulates the records of
+// kern_scatter_gpu1 and its siblings (every GCF size they accept: 8, 16, 32
+// and 64).  A call's kept records, counting-sorted by the kBlk x kBlk block of
+// their footprint corner (order_by_block), are cut into chunks of up to
+// ScatShape<S>::CH consecutive records (fewer for a call with few records),
+// one CTA per chunk.  A CTA accumulates the records of
 // one block at a time in shared memory, over the block's footprint region
 // ((kBlk + S - 1)^2 pixels), in the degridders' double-float arithmetic
 // (products and sums err by about 2^-48 of their size); each thread owns the
@@ -757,11 +758,11 @@ static int df_prepare(const double* grid, int32_t ext_x, int32_t ext_y, int64_t 
 // atomics of warp_scatter64 instead, so that those propagate as FP64 would.
 template <int S>
 struct ScatShape {
-  static constexpr int NT = S == 64 ? 1024 : 256;  // threads per CTA
+  static constexpr int NT = S == 64 ? 1024 : S == 8 ? 64 : 256;  // threads per CTA
   static constexpr int R = S * S / NT;            // residue slots per thread
   static constexpr int DR = NT / S;               // residue rows between a thread's slots
-  static constexpr int CH = S == 16 ? 512 : S == 32 ? 256 : 128;  // at most, records per CTA
-  static constexpr int CPS = S == 16 ? 5 : S == 32 ? 3 : 1;       // CTAs per SM (shared memory)
+  static constexpr int CH = S <= 16 ? 512 : S == 32 ? 256 : 128;  // at most, records per CTA
+  static constexpr int CPS = S == 8 ? 8 : S == 16 ? 5 : S == 32 ? 3 : 1;  // CTAs per SM
   static constexpr int RA = kBlk + S - 1;         // region edge (pixels)
   static constexpr int As = (RA + 7) & ~7;        // region row stride (float4)
 };
@@ -885,7 +886,7 @@ __global__ void __launch_bounds__(ScatShape<S>::NT)
 
 // Gridding of a call's n device records into the device grid `grid` (W x H,
 // rows W apart; zero, or zero on the blocks the records touch): the
-// shared-memory double-float kernel for GCF sizes 16, 32 and 64, the warp
+// shared-memory double-float kernel for GCF sizes 8, 16, 32 and 64, the warp
 // kernel with FP64 atomics otherwise.  Staging slots 5 (GCF split, exponents),
 // 7 and 8 (the records' order).
 static int scatter_records(int64_t n, const void* d_vis, const void* d_gcf, double2* grid,
@@ -893,7 +894,7 @@ static int scatter_records(int64_t n, const void* d_vis, const void* d_gcf, doub
   const int S = geo.S;
   int rc;
   if (!order && (rc = order_by_block(n, d_vis, geo, (int32_t**)&order, s))) return rc;
-  if (S != 16 && S != 32 && S != 64) {
+  if (S != 8 && S != 16 && S != 32 && S != 64) {
     int blocks;
     const int threads = plain_grid_dims(n, &blocks);
     k_scatter_single64<<<blocks, threads, 0, s>>>(n, (const double*)d_vis,
@@ -923,7 +924,7 @@ static int scatter_records(int64_t n, const void* d_vis, const void* d_gcf, doub
   if ((rc = stage_buffer(7, (size_t)3 * nkeys * sizeof(int32_t), &d_keys))) return rc;
   const int32_t* offs = (const int32_t*)d_keys + nkeys;
   // the shared-memory limit of each size's kernel, set once per device
-  static std::once_flag attr[3][64];
+  static std::once_flag attr[4][64];
   int dev = 0;
   GB_CUDA_TRY(cudaGetDevice(&dev));
   if (dev < 0 || dev >= 64) {
@@ -933,7 +934,7 @@ static int scatter_records(int64_t n, const void* d_vis, const void* d_gcf, doub
   auto launch = [&](auto tag) -> int {
     constexpr int SS = decltype(tag)::value;
     using Z = ScatShape<SS>;
-    std::call_once(attr[SS == 16 ? 0 : SS == 32 ? 1 : 2][dev], [] {
+    std::call_once(attr[SS == 8 ? 3 : SS == 16 ? 0 : SS == 32 ? 1 : 2][dev], [] {
       cudaFuncSetAttribute(k_scatter_blocks_df<SS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)scatter_blocks_smem<SS>());
     });
@@ -950,7 +951,8 @@ static int scatter_records(int64_t n, const void* d_vis, const void* d_gcf, doub
     GB_CUDA_TRY(cudaGetLastError());
     return GB_OK;
   };
-  return S == 16   ? launch(std::integral_constant<int, 16>{})
+  return S == 8    ? launch(std::integral_constant<int, 8>{})
+         : S == 16 ? launch(std::integral_constant<int, 16>{})
          : S == 32 ? launch(std::integral_constant<int, 32>{})
                    : launch(std::integral_constant<int, 64>{});
 }

@@ -135,3 +135,22 @@ def test_config1_slice_through_the_abi():
                               out) == 0
     ref = O.degrid(ob.scale, ob.grid_size, 8, gcf, exp, vis5)
     assert rel_l2(out[:, 3:], ref[:, 3:]) < TOL64
+
+
+@pytest.mark.parametrize("S", [8, 64])
+def test_degrid_single_and_out_of_bound_records(S):
+    """A call with one record (its taps then split over all the block's warps)
+    and a call whose records all fall outside the grid (copied through)."""
+    _, gcf = case(30 + S, n=10, S=S)
+    G = 256
+    grid = np.random.default_rng(4).standard_normal((G, G)) * (1 - 2j)
+    one = np.array([[3.3, -7.8, 1.0, 0.5, -0.25]])
+    out = np.zeros_like(one)
+    assert compat.call_degrid("kern_degrid_gpu1", 1.0, G, S, gcf, grid, one, out) == 0
+    exp = O.degrid(1.0, G, S, gcf, grid, one)
+    assert np.array_equal(out[:, :3], one[:, :3])
+    assert rel_l2(out[:, 3:], exp[:, 3:]) < TOL64
+    far = np.array([[1e9, 0.0, 0.0, 1.0, 2.0], [0.0, -1e9, 0.0, 3.0, 4.0], [5e8, 5e8, 1.0, 5.0, 6.0]])
+    out = np.zeros_like(far)
+    assert compat.call_degrid("kern_degrid_gpu1", 1.0, G, S, gcf, grid, far, out) == 0
+    assert np.array_equal(out, far)

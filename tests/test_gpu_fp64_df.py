@@ -153,11 +153,11 @@ def _abi_scatter(vis5, gcf, G, margin=64):
     return got, exp
 
 
-@pytest.mark.parametrize("S", [16, 32, 64])
+@pytest.mark.parametrize("S", [8, 16, 32, 64])
 @pytest.mark.parametrize("sv,sc", [(1e150, 1e-200), (2.0 ** -1000, 1.0), (1e-300, 1e300)])
 def test_reference_abi_scatter_extreme_magnitudes(S, sv, sc):
-    """The shared-memory double-float gridder behind kern_scatter_gpu1 (GCF
-    sizes 16, 32, 64) with visibilities and GCFs scaled far apart."""
+    """The shared-memory double-float gridder behind kern_scatter_gpu1 with
+    visibilities and GCFs scaled far apart."""
     vis5, gcf, G = _scatter_case(60 + S, S)
     vis5[:, 3:] *= sv
     got, exp = _abi_scatter(vis5, gcf * sc, G)
@@ -175,7 +175,7 @@ def test_reference_abi_scatter_forty_decades(S):
     assert rel_l2(got, exp) < TOL64
 
 
-@pytest.mark.parametrize("S", [16, 32, 64])
+@pytest.mark.parametrize("S", [8, 16, 32, 64])
 def test_reference_abi_scatter_nonfinite_and_subnormal(S):
     """A NaN visibility or an Inf GCF tap sends the call down the FP64
     atomics, which propagate them as the oracle does; so does a subnormal."""
