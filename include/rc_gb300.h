@@ -408,14 +408,14 @@ int gb_batch_degrid_f64(gb_batch *batch, const double *d_gcf, const double *cons
  * return GB_ERR_CAPACITY before any GPU work.  A grid more than 32767 tiles
  * wide or high returns GB_ERR_ARG, as gb_plan_create does.
  *
- * The first call on a device looks up the array's device address
- * (cudaGetSymbolAddress); make that first call before any stream capture.
- * The address is kept for the process: after cudaDeviceReset on a device, do
- * not call this entry point there again.
+ * The call synchronises `stream` once (to size the kernel launch), so it
+ * cannot be captured into a CUDA graph.  The first call on a device looks up
+ * the array's device address (cudaGetSymbolAddress) and keeps it for the
+ * process: after cudaDeviceReset on a device, do not call this entry point
+ * there again.
  * Every call on a device shares the array and leaves its contents behind; each
  * call clears what must start at zero.  Calls whose GPU work overlaps (other
- * streams, other host threads) race on the array: serialise them.  The call
- * synchronises `stream` once (to size the kernel launch). */
+ * streams, other host threads) race on the array: serialise them. */
 #define GB_NOALLOC_MAX_VIS (1 << 17)
 #define GB_NOALLOC_MAX_PIECES (1 << 18)
 #define GB_NOALLOC_MAX_BINS (1 << 16)
