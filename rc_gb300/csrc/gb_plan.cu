@@ -619,7 +619,7 @@ int gb::plan_create(const gb_geometry* geo, int64_t n_vis, const double* d_uvw,
   }
   // defaults: the measured best on the benchmark workloads (tile 24 with
   // 256 threads; pieces up to 40 x 40, so supports up to 40 stay whole and a
-  // CTA's accumulators still let three CTAs share an SM)
+  // CTA's accumulators still let four CTAs share an SM)
   const int T = geo->tile ? geo->tile : 24;
   const int NT = geo->threads ? geo->threads : 256;
   const int cap = geo->period_cap ? geo->period_cap : (40 * 40 <= 8 * NT ? 40 : 32);
