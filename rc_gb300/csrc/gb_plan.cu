@@ -207,6 +207,26 @@ static int dalloc(T** p, size_t n) {
   return rc;
 }
 
+// idx[0..n) reordered by cost, largest first, in one counting pass over the
+// costs quantised to 4096 levels of the largest (ties keep their order): the
+// longest-first heuristic needs no finer order, and a comparison sort of tens
+// of thousands of items costs milliseconds of host time per plan.
+static void order_by_cost(const std::vector<double>& cost, int32_t* idx, size_t n) {
+  if (n < 2) return;
+  constexpr int K = 4096;
+  double top = 0;
+  for (size_t i = 0; i < n; i++) top = std::max(top, cost[idx[i]]);
+  const double q = top > 0 ? (K - 1) / top : 0.0;
+  std::vector<int32_t> cnt(K + 1, 0), tmp(idx, idx + n);
+  auto level = [&](int32_t i) {
+    const int l = (int)(cost[i] * q);
+    return K - 1 - std::min(std::max(l, 0), K - 1);  // largest first
+  };
+  for (size_t i = 0; i < n; i++) cnt[level(tmp[i]) + 1]++;
+  for (int k = 1; k <= K; k++) cnt[k] += cnt[k - 1];
+  for (size_t i = 0; i < n; i++) idx[cnt[level(tmp[i])]++] = tmp[i];
+}
+
 void make_bundles(const std::vector<HostItem>& items, const ClassInfo* cls, int n_classes,
                   std::vector<Item>& it_out, std::vector<Bundle>& b_out) {
   // items by (class, grid slot), each bucket in the items' own order: one
@@ -229,15 +249,17 @@ void make_bundles(const std::vector<HostItem>& items, const ClassInfo* cls, int 
     double cost;
   };
   std::vector<HB> bundles;
+  bundles.reserve(items.size());
   it_out.clear();
   it_out.reserve(items.size());
-  const auto longer = [&](int32_t a, int32_t b) { return items[a].cost > items[b].cost; };
+  std::vector<double> cost(items.size());
+  for (size_t i = 0; i < items.size(); i++) cost[i] = items[i].cost;
   for (int c = 0; c < n_classes; c++) {
     const int G = cls[c].G;
     for (size_t g = 0; g < ng; g++) {
       const size_t k = (size_t)c * ng + g;
       if (first[k] == first[k + 1]) continue;
-      std::stable_sort(order.begin() + first[k], order.begin() + first[k + 1], longer);
+      order_by_cost(cost, order.data() + first[k], first[k + 1] - first[k]);
       for (size_t i = first[k]; i < first[k + 1]; i += G) {
         HB hb;
         hb.b.first_item = (int32_t)it_out.size();
@@ -252,11 +274,16 @@ void make_bundles(const std::vector<HostItem>& items, const ClassInfo* cls, int 
     }
   }
   // all bundles, longest first
-  std::stable_sort(bundles.begin(), bundles.end(),
-                   [](const HB& a, const HB& b) { return a.cost > b.cost; });
+  std::vector<int32_t> bo(bundles.size());
+  std::vector<double> bcost(bundles.size());
+  for (size_t i = 0; i < bo.size(); i++) {
+    bo[i] = (int32_t)i;
+    bcost[i] = bundles[i].cost;
+  }
+  order_by_cost(bcost, bo.data(), bo.size());
   b_out.clear();
   b_out.reserve(bundles.size());
-  for (auto& hb : bundles) b_out.push_back(hb.b);
+  for (int32_t i : bo) b_out.push_back(bundles[i].b);
 }
 
 // Modelled shared-memory wavefronts per pair that degridding's split-row stage
@@ -452,12 +479,12 @@ static int build_plan(gb_plan* P, const gb_geometry* geo, int64_t n_vis, const d
     const ClassInfo& ci = P->cls[c];
     return (double)(2 * ((ci.A * ci.A + ci.L - 1) / ci.L));
   };
+  // the histogram's cost per CTA slot (keys run rank-fastest within a tile)
+  std::vector<double> rank_w(nper);
+  for (int r = 0; r < nper; r++) rank_w[r] = rec_cost[r] / P->cls[rank_cls[r]].G;
   double total_cta = 0;
-  for (int64_t k = 0; k < nkeys; k++)
-    if (hist[k]) {
-      const int r = (int)(k % nper);
-      total_cta += hist[k] * rec_cost[r] / P->cls[rank_cls[r]].G;
-    }
+  for (int64_t k0 = 0; k0 < nkeys; k0 += nper)
+    for (int r = 0; r < nper; r++) total_cta += hist[k0 + r] * rank_w[r];
   const int ctas = std::max(1, sm_count() * std::max(1, P->ctas_per_sm_grid));
   const double tau = total_cta / ((double)P->bpc * ctas);
   // a class's periods are consecutive ranks (group width grows with the period)
