@@ -13,6 +13,7 @@
 //   3. k_plan_fill: recompute the index, scatter 16-byte records into their
 //      bins.
 #include <algorithm>
+#include <thread>
 #include <cstdlib>
 #include <cstring>
 #include <numeric>
@@ -510,59 +511,93 @@ static int build_plan(gb_plan* P, const gb_geometry* geo, int64_t n_vis, const d
       }
     }
   }
-  std::vector<HostItem> items;
-  int64_t top_taps = 0;
-  int top_rank = -1;
-  auto close_item = [&](HostItem& h) {
-    h.it.cls = item_cls_with_residue(h.it.cls, top_rank < 0 ? -1 : rank_residue[top_rank]);
-    top_taps = 0;
-    top_rank = -1;
-    items.push_back(h);
-  };
-  int64_t tiles_used = 0;
-  for (int64_t tile = 0; tile < (int64_t)P->ntx * P->nty; tile++) {
-    const int64_t k0 = tile * nper;
-    if (offs[k0 + nper] == offs[k0]) continue;
-    tiles_used++;
-    const int16_t tx = (int16_t)(tile % P->ntx), ty = (int16_t)(tile / P->ntx);
-    for (int c = 0; c < P->n_classes; c++) {
-      if (r_lo[c] >= r_hi[c] || offs[k0 + r_hi[c]] == offs[k0 + r_lo[c]]) continue;
-      const double fixed = fixed_cost(c), cmax = std::max(4.0 * fixed, tau);
-      HostItem cur{};
-      bool open = false;
-      for (int r = r_lo[c]; r < r_hi[c]; r++) {
-        int32_t pos = offs[k0 + r];
-        const int32_t end = offs[k0 + r + 1];
-        const double rcst = rec_cost[r];
-        while (pos < end) {
-          if (!open) {
-            cur.it.start = pos;
-            cur.it.count = 0;
-            cur.it.tile_x = tx;
-            cur.it.tile_y = ty;
-            cur.it.pmax = 0;
-            cur.it.cls = (int16_t)c;
-            cur.cost = fixed;
-            open = true;
-          }
-          int64_t room = (int64_t)((cmax - cur.cost) / rcst);
-          if (room < 1) room = 1;
-          const int32_t take = (int32_t)std::min<int64_t>(room, end - pos);
-          cur.it.count += take;
-          cur.it.pmax = (int16_t)std::max<int>(cur.it.pmax, periods[r]);
-          cur.cost += take * rcst;
-          if ((int64_t)take * periods[r] * periods[r] > top_taps) {
-            top_taps = (int64_t)take * periods[r] * periods[r];
-            top_rank = r;
-          }
-          pos += take;
-          if (cur.cost >= cmax) {
-            close_item(cur);
-            open = false;
+  // items of tiles [t0, t1) in tile order, into out
+  auto build_items = [&](int64_t t0, int64_t t1, std::vector<HostItem>& out, int64_t& used) {
+    int64_t top_taps = 0;
+    int top_rank = -1;
+    auto close_item = [&](HostItem& h) {
+      h.it.cls = item_cls_with_residue(h.it.cls, top_rank < 0 ? -1 : rank_residue[top_rank]);
+      top_taps = 0;
+      top_rank = -1;
+      out.push_back(h);
+    };
+    for (int64_t tile = t0; tile < t1; tile++) {
+      const int64_t k0 = tile * nper;
+      if (offs[k0 + nper] == offs[k0]) continue;
+      used++;
+      const int16_t tx = (int16_t)(tile % P->ntx), ty = (int16_t)(tile / P->ntx);
+      for (int c = 0; c < P->n_classes; c++) {
+        if (r_lo[c] >= r_hi[c] || offs[k0 + r_hi[c]] == offs[k0 + r_lo[c]]) continue;
+        const double fixed = fixed_cost(c), cmax = std::max(4.0 * fixed, tau);
+        HostItem cur{};
+        bool open = false;
+        for (int r = r_lo[c]; r < r_hi[c]; r++) {
+          int32_t pos = offs[k0 + r];
+          const int32_t end = offs[k0 + r + 1];
+          const double rcst = rec_cost[r];
+          while (pos < end) {
+            if (!open) {
+              cur.it.start = pos;
+              cur.it.count = 0;
+              cur.it.tile_x = tx;
+              cur.it.tile_y = ty;
+              cur.it.pmax = 0;
+              cur.it.cls = (int16_t)c;
+              cur.cost = fixed;
+              open = true;
+            }
+            int64_t room = (int64_t)((cmax - cur.cost) / rcst);
+            if (room < 1) room = 1;
+            const int32_t take = (int32_t)std::min<int64_t>(room, end - pos);
+            cur.it.count += take;
+            cur.it.pmax = (int16_t)std::max<int>(cur.it.pmax, periods[r]);
+            cur.cost += take * rcst;
+            if ((int64_t)take * periods[r] * periods[r] > top_taps) {
+              top_taps = (int64_t)take * periods[r] * periods[r];
+              top_rank = r;
+            }
+            pos += take;
+            if (cur.cost >= cmax) {
+              close_item(cur);
+              open = false;
+            }
           }
         }
+        if (open) close_item(cur);
       }
-      if (open) close_item(cur);
+    }
+  };
+  // tiles in contiguous chunks on up to eight host threads, concatenated in
+  // tile order (the same items as one thread makes)
+  const int64_t ntiles = (int64_t)P->ntx * P->nty;
+  const int nth = (int)std::clamp<int64_t>(ntiles / 8192, 1,
+                                           std::min(8u, std::max(1u, std::thread::hardware_concurrency())));
+  std::vector<std::vector<HostItem>> parts(nth);
+  std::vector<int64_t> used(nth, 0);
+  {
+    std::vector<std::thread> pool;
+    for (int i = 1; i < nth; i++) {
+      try {
+        pool.emplace_back(build_items, ntiles * i / nth, ntiles * (i + 1) / nth, std::ref(parts[i]),
+                          std::ref(used[i]));
+      } catch (...) {  // no thread: this one does that chunk below
+        break;
+      }
+    }
+    build_items(0, ntiles / nth, parts[0], used[0]);
+    for (auto& t : pool) t.join();
+    for (int i = (int)pool.size() + 1; i < nth; i++)
+      build_items(ntiles * i / nth, ntiles * (i + 1) / nth, parts[i], used[i]);
+  }
+  std::vector<HostItem> items;
+  int64_t tiles_used = 0;
+  {
+    size_t total = 0;
+    for (auto& v : parts) total += v.size();
+    items.reserve(total);
+    for (int i = 0; i < nth; i++) {
+      items.insert(items.end(), parts[i].begin(), parts[i].end());
+      tiles_used += used[i];
     }
   }
   P->tiles_used = tiles_used;
